@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Particle-steps/s of sphugo's 2D SPH step on GB300.
+
+Workload (the plain-FP64-at-scale case): N = 1,048,576 particles uniform in the
+periodic unit box, blast u = 10 inside r < 0.1 (else 1), k = 32, Monahan
+kernel, gamma 5/3, alpha 1, beta 2, dt = 2e-5, seeded SplitMix64 inputs.
+`value` is the plain FP64 drop-in (SPH_PREC_FP64, bit-exact with the
+reference's arithmetic) timed with CUDA events on the library's stream over K
+steps after W warm-up steps, inputs resident in HBM (state > 1 GB, larger than
+L2). `e2e` times the same steps through the public C ABI with the whole state
+copied host->device and back every step from pinned host buffers. Extra
+lines of the JSON report the FP64-fast and mixed forms and the 256-simulation
+ensemble, each against the stated tolerances that the test-suite enforces.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank advances its own replica (a single
+simulation does not shard without a halo exchange): value = all ranks'
+particle-steps / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 1_048_576
+K_NEIGH = 32
+DT = 2e-5
+SEED = 2
+METRIC = "particle-steps/s on 1 GB300: mixed/batched vs plain FP64 GPU at stated rel. error"
+TOLERANCES = {"neighbour_sets": "bit-exact", "fp64": "bit-exact", "fp64_fast": 1e-12,
+              "mixed_rho": 1e-5, "mixed_accel_normalised": 1e-4, "mixed_udot_normalised": 1e-4}
+
+# Algorithmic work per particle and force evaluation at k = 32:
+# bytes for the streaming stages, FP64 flops (adds, multiplies, divisions and
+# square roots of the reference formulas, 1 flop each) for the FP64 stages.
+def algorithmic(k):
+    return {
+        "bin": {"bytes": 32 + 8, "unit": "GB/s"},
+        "scan": {"bytes": None, "unit": "GB/s"},  # per cell: 16 B, filled in below
+        "permute": {"bytes": 76 + 8 + 4 + 92, "unit": "GB/s"},
+        "knn_density": {"fp64_flops": 7 * (k + 1) + 8 * k + 12, "bytes": 16 + 4 * k + 8 * k + 56,
+                        "unit": "TFLOP/s"},
+        "force_integrate": {"fp64_flops": 34 * k + 30, "bytes": 80 + 4 * k + 8 * k, "unit": "TFLOP/s"},
+    }
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max-over-ranks for torchrun launches (gloo, CPU tensors)."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = env_rank()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def max_over_ranks(values):
+    """Reduction the timed region uses (max over ranks)."""
+    return max(values)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def make_sim(n, precision, seed):
+    from sphugo_gb300 import ics
+    from sphugo_gb300 import sim as S
+    conf = ics.periodic_config(n, K_NEIGH, DT, precision)
+    arrs = ics.uniform_blast(n, seed)
+    return S.Simulation(conf, *arrs)
+
+
+def timed(sim, steps):
+    from sphugo_gb300 import _lib as L
+    ms = C.c_double(0)
+    L.check(L.load().sph_step_timed(sim._h, steps, C.byref(ms)))
+    return ms.value
+
+
+def profile(sim, steps=3):
+    from sphugo_gb300 import _lib as L
+    import numpy as np
+    out = np.zeros(L.NUM_STAGES)
+    L.check(L.load().sph_step_profiled(sim._h, steps, L.dptr(out)))
+    return dict(zip(L.STAGES, out.tolist()))
+
+
+def e2e_run(sim, steps):
+    """set_state from pinned host arrays + step + get_state, every step."""
+    import numpy as np
+    from sphugo_gb300 import _lib as L
+    lib = L.load()
+    n = sim.n
+    bufs = [np.empty(n) for _ in range(8)]
+    for b in bufs:
+        L.check(lib.sph_host_register(b.ctypes.data, b.nbytes))
+    try:
+        st = sim.state()
+        for b, k in zip(bufs, ["x", "y", "vx", "vy", "u", "ax", "ay", "udot"]):
+            b[:] = st[k]
+        ptrs = [L.dptr(b) for b in bufs]
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            L.check(lib.sph_set_state(sim._h, *ptrs))
+            L.check(lib.sph_step(sim._h, 1))
+            L.check(lib.sph_get_state(sim._h, *ptrs))
+        dt = time.perf_counter() - t0
+    finally:
+        for b in bufs:
+            lib.sph_host_unregister(b.ctypes.data)
+    return dt, 8 * 8 * n, 8 * 8 * n
+
+
+def cpu_baseline(n, steps, threads, warm=1):
+    """The oracle's faithful tree path (restating the reference's Step) on host cores."""
+    from oracle import oracle as O
+    from sphugo_gb300 import ics
+    x, y, vx, vy, u = ics.uniform_blast(n, SEED)
+    s = O.OracleSim(O.make_params(n, K_NEIGH, knn_mode=O.KNN_TREE, threads=threads, alpha=1.0, beta=2.0,
+                                  dth=DT / 2), x, y, vx, vy, u)
+    s.step(warm)  # step 0 evaluates forces twice; time regular steps only
+    t0 = time.perf_counter()
+    s.step(steps)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, dist):
+    """--impl reference: the reference's CPU algorithm (oracle port, all cores)."""
+    if dist.rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n = args.n or N_DEFAULT
+    warm = max(1, args.warmup)
+    steps = max(1, args.steps)
+    secs = cpu_baseline(n, steps, threads, warm=warm)
+    v = n * steps / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+        "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}",
+                   "n": n, "k": K_NEIGH, "form": "reference tree search, FP64"},
+        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} full steps of N={n} after {warm} warm-up steps"},
+        "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=0, help="override the particle count (testing only)")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+def run_ours(args, dist):
+    from sphugo_gb300 import _lib as L
+    from sphugo_gb300 import build
+    build.build()
+    lib = L.load()
+    n = args.n or N_DEFAULT
+    K, W = max(1, args.steps), max(3, args.warmup)
+    fp64_pk, fp32_pk = C.c_double(0), C.c_double(0)
+    L.check(lib.sph_probe_peaks(C.byref(fp64_pk), C.byref(fp32_pk)))
+
+    sim = make_sim(n, "Exact", SEED + 1000 * dist.rank)
+    sim.Step(W)
+    kernels = int(lib.sph_kernels_per_step(sim._h))
+    clk = ClockSampler(dist.local)
+    clk.start()
+    dist.barrier()
+    ms = timed(sim, K)
+    dist.barrier()
+    clocks = clk.stop()
+    ms_max = dist.max(ms)
+    value = n * K * dist.world / (ms_max / 1e3)
+
+    stages = profile(sim, 3)
+    work = algorithmic(K_NEIGH)
+    ncells = 4 ** 10  # auto level for N = 2^20
+    dom = max(stages, key=stages.get)
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    roof = {}
+    for st, t in stages.items():
+        w = work[st]
+        entry = {"ms": t}
+        if "fp64_flops" in w:
+            entry.update(bound="fp64", unit="TFLOP/s", achieved=w["fp64_flops"] * n / (t * 1e-3) / 1e12,
+                         peak=fp64_pk.value)
+        else:
+            b = w["bytes"] * n if w["bytes"] else 16 * ncells
+            entry.update(bound="hbm", unit="GB/s", achieved=b / (t * 1e-3) / 1e9, peak=hbm_peak)
+        if entry.get("peak"):
+            entry["frac"] = entry["achieved"] / entry["peak"]
+        roof[st] = entry
+    d = roof[dom]
+    roofline = {"kernel": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
+                "unit": d["unit"], "frac": d.get("frac"), "traffic": None,
+                "peak_source": ("FP64 FMA probe run by this bench (MEASURED_PEAKS.json has no FP64 figure)"
+                                if d["bound"] == "fp64" else "MEASURED_PEAKS.json hbm_gbs"),
+                "stages": roof}
+
+    dt, h2d, d2h = e2e_run(sim, max(3, K // 2))
+    e2e = {"value": n * max(3, K // 2) / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+    sim.close()
+
+    extras = {}
+    if not args.no_extras and dist.rank == 0:
+        for form in ("Fast", "Mixed"):
+            s2 = make_sim(n, form, SEED)
+            s2.Step(W)
+            t = timed(s2, K)
+            extras[{"Fast": "fp64_fast", "Mixed": "mixed"}[form]] = {
+                "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3)}
+            s2.close()
+        extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
+
+    cpu = None
+    if not args.no_cpu and dist.rank == 0:
+        threads = os.cpu_count() or 1
+        ncpu = n
+        secs = cpu_baseline(ncpu, 2, threads)
+        cpu = {"value": ncpu * 2 / secs, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": f"2 regular steps of the same workload (N={ncpu}) through the oracle's tree path"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": dist.world, "steps": K,
+            "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 uniform blast)",
+            "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}, plain FP64",
+                       "n": n, "k": K_NEIGH, "form": "SPH_PREC_FP64 (bit-exact)", "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (state + neighbour lists > 1 GB)"},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": kernels * K, "kernels_per_step": kernels,
+            "roofline": roofline, "cpu_baseline": cpu, "tolerances": TOLERANCES,
+            "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value}, "forms": extras,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,232 @@
+/*
+ * sphgpu.h -- C ABI of the GB300-native SPH step (libsphgpu.so).
+ *
+ * This is the drop-in boundary under the Go package sim of bbeni/sphugo: each
+ * entry point replaces one piece of the reference's Go API (cited per
+ * function, paths within that project). A cgo shim binds these directly; the
+ * library owns all device memory, keeps particle state resident in HBM between
+ * calls and copies the caller's host arrays in and out, so the caller keeps
+ * ownership of its buffers. Every function returns an int status (0 = ok,
+ * negative = error class) and leaves a message for sph_last_error().
+ * Plain pointers and sizes only; nothing here depends on a GPU being present
+ * until a handle is created.
+ */
+#ifndef SPHGPU_H
+#define SPHGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGPU_ABI_VERSION 1
+
+/* status codes */
+#define SPH_OK 0
+#define SPH_ERR_ARG -1        /* invalid argument (the reference would panic or misbehave) */
+#define SPH_ERR_CUDA -2       /* CUDA runtime error / no device */
+#define SPH_ERR_NOMEM -3      /* device allocation failed */
+#define SPH_ERR_KNN -4        /* neighbour search failed (see sph_last_error) */
+#define SPH_ERR_SENTINEL -5   /* a k-th neighbour lies beyond the reference's 0.4 queue sentinel */
+#define SPH_ERR_RANGE -6      /* q = r/h outside [0,1] or non-finite state */
+#define SPH_ERR_CONFIG -7     /* .sph-config parse / validation error */
+#define SPH_ERR_STATE -8      /* call out of order (e.g. step before upload) */
+
+/* kernels: sim/sph.go:258 Monahan2D, sim/sph.go:284 Wendtland2D */
+#define SPH_KERNEL_MONAHAN 0
+#define SPH_KERNEL_WENDLAND 1
+
+/* arithmetic form of density and force */
+#define SPH_PREC_FP64 0       /* plain FP64 drop-in: the reference's operation order, bit for bit */
+#define SPH_PREC_MIXED 1      /* FP32 relative-coordinate sums with compensation; FP64 kNN decisions, h and integrator */
+#define SPH_PREC_FP64_FAST 2  /* FP64 with contraction and per-particle reciprocals (within 1e-12 of SPH_PREC_FP64) */
+
+/* Simulation parameters: the fields of SphConfig that the step reads
+ * (sim/config-parser.go:111-128) plus the constants the reference hard-codes
+ * (NN_SIZE sim/core.go:14; alpha, beta, etaSq sim/sph.go:379-383). */
+typedef struct sph_params {
+    int32_t k;           /* neighbours per particle (NN_SIZE), 1..128 */
+    int32_t kernel;      /* SPH_KERNEL_* (SphConfig.Kernel) */
+    int32_t precision;   /* SPH_PREC_* */
+    int32_t grid_level;  /* finest binning level (cells per axis = 2^level); 0 = automatic */
+    double gamma;        /* SphConfig.Gamma */
+    double mass;         /* SphConfig.ParticleMass */
+    double dth;          /* SphConfig.DeltaTHalf */
+    double accel[2];     /* SphConfig.Acceleration */
+    double hor[2];       /* SphConfig.HorPeriodicity; {-DBL_MAX, DBL_MAX} = open */
+    double vert[2];      /* SphConfig.VertPeriodicity */
+    double refl[4];      /* SphConfig.Reflections L, R, U, D */
+    double alpha, beta, etasq; /* artificial viscosity (reference: 0.75, 1.5, 0.01) */
+} sph_params;
+
+typedef struct sph_handle sph_handle;
+
+/* Defaults of sim/config-parser.go:131-149 MakeConfig (open bounds, gamma
+ * 1.66666, mass 1, DeltaTHalf 0.001, Monahan) with k = 32 and the
+ * reference's viscosity constants. */
+sph_params sph_default_params(void);
+
+/* Library / device info. */
+int32_t sph_abi_version(void);
+const char *sph_last_error(void);           /* thread-local message of the last failure */
+int sph_device_count(int32_t *count);
+
+/* ---- lifetime ---- */
+/* One simulation of n particles. Replaces sim/sph.go:41 MakeSimulationFromConf
+ * (the particles themselves come with sph_upload). */
+int sph_create(const sph_params *p, int64_t n, sph_handle **out);
+/* An ensemble of nsims independent simulations advanced together, each with
+ * its own parameters and particle count; particle arrays passed to the other
+ * calls are the concatenation of the simulations in order. k and precision
+ * must agree across the ensemble. No reference counterpart (the reference
+ * runs one Simulation per process). */
+int sph_ens_create(const sph_params *params, const int64_t *counts, int32_t nsims, sph_handle **out);
+int sph_destroy(sph_handle *h);
+
+/* ---- state transfer (host arrays in the caller's particle order) ---- */
+/* Sets positions, velocities and specific internal energies and resets the
+ * step counter to 0, as building Root.Particles does (sim/sph.go:41-53).
+ * vx, vy, u may be NULL (zero). */
+int sph_upload(sph_handle *h, const double *x, const double *y, const double *vx,
+               const double *vy, const double *u);
+/* Replaces the full integrator state (including the last accelerations and
+ * du/dt that the next drift reads) without touching the step counter, for a
+ * caller that owns the state on the host between steps. */
+int sph_set_state(sph_handle *h, const double *x, const double *y, const double *vx,
+                  const double *vy, const double *u, const double *ax, const double *ay,
+                  const double *udot);
+/* Particle.Pos, Vel, E, VDot, EDot; any pointer may be NULL. */
+int sph_get_state(sph_handle *h, double *x, double *y, double *vx, double *vy, double *u,
+                  double *ax, double *ay, double *udot);
+/* Particle.Rho, C and NNDists[0] (the smoothing length) of the last force
+ * evaluation; any pointer may be NULL. */
+int sph_get_derived(sph_handle *h, double *rho, double *c, double *hsml);
+/* Particle.NearestNeighbours / NNDists in the reference layout
+ * (sim/core.go:36-38): n*k entries, slot 0 = the farthest neighbour; ids are
+ * particle indices in the caller's order; dist may be NULL; img (may be
+ * NULL) is the periodic image code (i+1)*3+(j+1) of the offset (i*dX, j*dY)
+ * used by sim/nearest-neighbour.go:57-61. */
+int sph_get_neighbours(sph_handle *h, int64_t *ids, double *dist, int32_t *img);
+
+/* ---- stepping ---- */
+/* sim/sph.go:64 (*Simulation).Step, nsteps times; step 0 performs the extra
+ * force evaluation of sim/sph.go:89-103. Runs as captured CUDA graphs. */
+int sph_step(sph_handle *h, int32_t nsteps);
+/* sim/sph.go:403 CalculateForces on the current positions and predicted
+ * velocities / energies (without integrating). */
+int sph_forces(sph_handle *h);
+int sph_synchronize(sph_handle *h);
+int32_t sph_current_step(const sph_handle *h);
+int64_t sph_num_particles(const sph_handle *h);
+
+/* ---- measurement (no reference counterpart) ---- */
+#define SPH_NUM_STAGES 5   /* bin (incl. prep/bbox), scan, permute, knn+density, force+integrate */
+/* sph_step with the device time between CUDA events recorded on the
+ * handle's stream before the first and after the last step, in ms. */
+int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms);
+/* nsteps steps (step 0's extra evaluation excluded from the timing) through
+ * a graph that carries event nodes between the stages; stage_ms receives the
+ * per-step mean device time of each stage. */
+int sph_step_profiled(sph_handle *h, int32_t nsteps, double stage_ms[SPH_NUM_STAGES]);
+/* Kernel launches of one regular step (graph kernel nodes). */
+int32_t sph_kernels_per_step(sph_handle *h);
+/* Arithmetic throughput probe on the current device: FP64 FMA and FP32 FMA
+ * in TFLOP/s (2 flops per FMA), from independent FMA chains. */
+int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops);
+
+/* Page-locks (pins) caller memory so that transfers from / to it run at
+ * full link speed; no reference counterpart. */
+int sph_host_register(void *ptr, int64_t bytes);
+int sph_host_unregister(void *ptr);
+
+/* ---- diagnostics (sim/sph.go:441-463) ----
+ * out[0] = TotalEnergy (sum E), out[1] = TotalDensity (sum rho),
+ * out[2] = TotalMomentum as the reference computes it (the norm of the last
+ * particle's velocity: its loop assigns instead of adding),
+ * out[3] = sum of |v| (the intended total). For an ensemble, sim selects one
+ * simulation (-1 = all particles). */
+int sph_diagnostics(sph_handle *h, int32_t sim, double out[4]);
+
+/* ---- synthetic initial conditions (host only; no GPU needed) ----
+ * SplitMix64 stream, 53-bit uniform doubles in [0,1). */
+/* Uniform positions in [0,1)^2, v = 0, u = u_blast inside the disc of
+ * radius r_blast about (0.5,0.5), u_bg elsewhere. */
+int sph_ic_uniform_blast(int64_t n, uint64_t seed, double u_bg, double u_blast, double r_blast,
+                         double *x, double *y, double *vx, double *vy, double *u);
+/* nblobs Gaussian blobs (centres U[0,1)^2, sigma log-uniform in
+ * [sig_min, sig_max], wrapped periodically) holding (1-f_bg) of the
+ * particles in equal shares, plus f_bg uniform background; u = u_core inside
+ * sigma of the own blob centre, u_bg elsewhere. */
+int sph_ic_clustered(int64_t n, uint64_t seed, int32_t nblobs, double sig_min, double sig_max,
+                     double f_bg, double u_bg, double u_core,
+                     double *x, double *y, double *vx, double *vy, double *u);
+/* f_in of the particles uniform in a side x side square at a uniform random
+ * offset in [0, 1-side)^2, the rest uniform outside it; u = u_hot within
+ * r_hot of the square centre, u_bg elsewhere. */
+int sph_ic_stress(int64_t n, uint64_t seed, double side, double f_in, double u_bg, double u_hot,
+                  double r_hot, double *x, double *y, double *vx, double *vy, double *u);
+/* Ensemble sizes log-uniform in [nmin, nmax] and per-simulation blast
+ * energies uniform in [ublo, ubhi]. */
+int sph_ic_ensemble(int32_t nsims, uint64_t seed, int64_t nmin, int64_t nmax, double ublo,
+                    double ubhi, int64_t *counts, double *u_blast);
+
+/* ---- .sph-config setup (sim/config-parser.go) ---- */
+#define SPH_CONFIG_MAX_SPAWNERS 64
+
+/* [[Start]] [UniformRect] (sim/config-parser.go:37-41) */
+typedef struct sph_rect_spawner {
+    double upper_left[2];
+    double lower_right[2];
+    int64_t n;
+} sph_rect_spawner;
+
+/* [[Sources]] [Point] (sim/config-parser.go:43-47) */
+typedef struct sph_point_source {
+    double origin[2];
+    double rate;
+    double last_spawned;
+} sph_point_source;
+
+/* SphConfig (sim/config-parser.go:111-128) with the fields this library adds
+ * (k, viscosity constants, precision, grid level) inside params. */
+typedef struct sph_config {
+    sph_params params;
+    int32_t nsteps;                  /* NSteps */
+    int32_t nstart;                  /* number of start spawners */
+    int32_t nsources;                /* number of point sources */
+    int32_t pad_;
+    double viewport[4];              /* Viewport UpperLeft (x,y), LowerRight (x,y) */
+    sph_rect_spawner start[SPH_CONFIG_MAX_SPAWNERS];
+    sph_point_source sources[SPH_CONFIG_MAX_SPAWNERS];
+} sph_config;
+
+/* sim/config-parser.go:131 MakeConfig defaults. */
+void sph_config_default(sph_config *out);
+/* sim/config-parser.go:151 MakeConfigFromFile: tokenises and validates a
+ * .sph-config file with the reference's grammar; on failure returns
+ * SPH_ERR_CONFIG, writes the reference-format message
+ * "file:line:col: ConfigParseError|ConfigMakeError: ..." into err and resets
+ * *out to the defaults. Extra keys under [[Simulation]] [Config]:
+ * NeighbourCount (int), ViscosityAlpha, ViscosityBeta, ViscosityEtaSq
+ * (float), Precision (a word: Exact = SPH_PREC_FP64, Fast =
+ * SPH_PREC_FP64_FAST, Mixed = SPH_PREC_MIXED), GridLevel (int). */
+int sph_config_load(const char *path, sph_config *out, char *err, int32_t errlen);
+/* Total particles of all start spawners. */
+int64_t sph_config_start_count(const sph_config *cfg);
+/* UniformRectSpawner.Spawn(0) of every start spawner in order
+ * (sim/config-parser.go:58-80): the generator is reseeded with 12345678 at
+ * each spawner, as the reference reseeds math/rand; E = 0.01, v = 0.
+ * Arrays hold sph_config_start_count() entries; vx, vy, u may be NULL. */
+int sph_config_spawn(const sph_config *cfg, double *x, double *y, double *vx, double *vy, double *u);
+/* PointSource.Spawn(t) (sim/config-parser.go:82-102): returns how many
+ * particles the source emits at time t (int(deltaT / cooldown)), advances its
+ * last_spawned clock, and when x/y are not NULL fills them (origin +- 0.01
+ * uniform, seeded by seed) with u = 0.002 and v = 0. */
+int64_t sph_point_source_spawn(sph_point_source *src, double t, uint64_t seed, double *x, double *y,
+                               double *vx, double *vy, double *u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,672 @@
+// api.cu -- the C ABI of include/sphgpu.h: handle lifetime, device memory
+// layout, host <-> device transfers and the per-step CUDA graphs.
+//
+// A handle mirrors the reference's Simulation (sim/sph.go:14-21): its mutex
+// plays the role of Simulation.IsBusy, it owns the particle state (kept
+// resident in HBM) and counts steps. Each force evaluation is the kernel
+// chain prep -> [bbox -> grid] -> bin -> scan -> permute -> knn -> force,
+// captured once into a CUDA graph per integration mode and replayed.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+using namespace sphgpu;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                    \
+    do {                                                                               \
+        cudaError_t e_ = (x);                                                          \
+        if (e_ != cudaSuccess)                                                         \
+            return fail(e_ == cudaErrorMemoryAllocation ? SPH_ERR_NOMEM : SPH_ERR_CUDA, \
+                        std::string(#x) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+// Kernel prefactors of sim/sph.go:266,275,293,303, correctly rounded (Go folds
+// the constant expressions in exact arithmetic).
+const double kMonahanPref = 0x1.5d3b3e3583243p+3;
+const double kWendFPref = 0x1.1d34a60108f72p+1;
+const double kWendDFPref = 0x1.1d34a60108f72p+2;
+
+int auto_level(int64_t n) {
+    // about one to four particles per finest cell
+    double l = std::floor(0.5 * std::log2(std::max<double>((double)n, 2.0) / 2.0) + 0.5);
+    return (int)std::min<double>(std::max<double>(l, 1.0), kMaxLevel);
+}
+}  // namespace
+
+struct sph_handle {
+    int device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    int nsims = 0, k = 32, mode = MODE_EXACT64;
+    int64_t n = 0;
+    std::vector<sph_params> params;
+    std::vector<int64_t> offs;
+    std::vector<SimDev> hsims;
+    SimDev *d_sims = nullptr;
+    int64_t *d_offs = nullptr;
+    unsigned *d_flags = nullptr;
+    PArrays A{}, B{};
+    Derived D{};
+    Tables T{};
+    KnnTune tune{};
+    bool any_open = false, uploaded = false, evaluated = false;
+    int32_t step = 0;
+    cudaGraphExec_t g_step = nullptr, g_init = nullptr, g_forces = nullptr, g_prof = nullptr;
+    cudaEvent_t ev[SPH_NUM_STAGES + 1] = {};
+    int kernels_per_step = 0;
+    double *d_io = nullptr;   // transfer / reduction staging
+    size_t io_doubles = 0;
+    void *d_nbr_io = nullptr; // neighbour export staging (lazy)
+    std::vector<void *> allocs;
+    std::mutex mu;
+
+    Ctx ctx() const {
+        Ctx c;
+        c.sims = d_sims;
+        c.sims_rw = d_sims;
+        c.offs = d_offs;
+        c.nsims = nsims;
+        c.n = n;
+        c.k = k;
+        c.flags = d_flags;
+        return c;
+    }
+    Launch launch() const { return Launch{sms, stream}; }
+};
+
+namespace {
+
+template <typename T>
+int dalloc(sph_handle *h, T **p, size_t count) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? SPH_ERR_NOMEM : SPH_ERR_CUDA,
+                    std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    h->allocs.push_back(q);
+    *p = (T *)q;
+    return SPH_OK;
+}
+
+int alloc_parrays(sph_handle *h, PArrays &P, bool mixed) {
+    int64_t n = h->n;
+    int rc = 0;
+    rc |= dalloc(h, &P.pos, n);
+    rc |= dalloc(h, &P.vel, n);
+    rc |= dalloc(h, &P.vp, n);
+    rc |= dalloc(h, &P.acc, n);
+    rc |= dalloc(h, &P.u, n);
+    rc |= dalloc(h, &P.up, n);
+    rc |= dalloc(h, &P.udot, n);
+    rc |= dalloc(h, &P.id, n);
+    rc |= dalloc(h, &P.hprev, n);
+    rc |= dalloc(h, &P.rec, n);
+    if (mixed) rc |= dalloc(h, &P.vrec, n);
+    return rc ? SPH_ERR_NOMEM : SPH_OK;
+}
+
+int check_params(const sph_params &p, int64_t n) {
+    if (p.k < 1 || p.k > 128) return fail(SPH_ERR_ARG, "k must be in [1, 128]");
+    if (n < (int64_t)p.k + 1) return fail(SPH_ERR_ARG, "a simulation needs at least k+1 particles");
+    if (p.kernel != SPH_KERNEL_MONAHAN && p.kernel != SPH_KERNEL_WENDLAND)
+        return fail(SPH_ERR_ARG, "unknown kernel");
+    if (p.precision < 0 || p.precision > 2) return fail(SPH_ERR_ARG, "unknown precision");
+    if (p.grid_level < 0 || p.grid_level > kMaxLevel) return fail(SPH_ERR_ARG, "grid_level must be in [0, 14]");
+    const double *ax[2] = {p.hor, p.vert};
+    for (int a = 0; a < 2; a++) {
+        // sim/nearest-neighbour.go:39-55 panics on a half-open axis
+        if (ax[a][0] == -DBL_MAX) {
+            if (ax[a][1] != DBL_MAX) return fail(SPH_ERR_ARG, "cannot have open and periodic boundary on one axis");
+        } else if (!(ax[a][1] > ax[a][0]) || !std::isfinite(ax[a][1] - ax[a][0])) {
+            return fail(SPH_ERR_ARG, "periodic bounds must satisfy lo < hi");
+        }
+    }
+    if (!std::isfinite(p.dth) || !std::isfinite(p.gamma) || !std::isfinite(p.mass))
+        return fail(SPH_ERR_ARG, "non-finite parameter");
+    return SPH_OK;
+}
+
+SimDev make_simdev(const sph_params &p, int64_t off, int64_t n, int64_t cell_off, int level) {
+    SimDev S;
+    memset(&S, 0, sizeof S);
+    S.off = off;
+    S.n = n;
+    S.cell_off = cell_off;
+    S.level = level;
+    S.kernel = p.kernel;
+    const double *ax[2] = {p.hor, p.vert};
+    int G = 1 << level;
+    for (int a = 0; a < 2; a++) {
+        S.per_lo[a] = ax[a][0];
+        S.per_hi[a] = ax[a][1];
+        S.periodic[a] = ax[a][0] != -DBL_MAX;
+        if (S.periodic[a]) {
+            S.lo[a] = ax[a][0];
+            S.L[a] = ax[a][1] - ax[a][0];
+            S.dimg[a] = ax[a][1] - ax[a][0];
+        } else {
+            S.lo[a] = 0.0;
+            S.L[a] = 1.0;
+            S.dimg[a] = 0.0;
+        }
+        S.s[a] = S.L[a] / G;
+        S.inv_s[a] = G / S.L[a];
+    }
+    S.gamma = p.gamma;
+    S.mass = p.mass;
+    S.dth = p.dth;
+    S.accel[0] = p.accel[0];
+    S.accel[1] = p.accel[1];
+    for (int i = 0; i < 4; i++) S.refl[i] = p.refl[i];
+    S.alpha = p.alpha;
+    S.beta = p.beta;
+    S.etasq = p.etasq;
+    S.fpref = p.kernel == SPH_KERNEL_WENDLAND ? kWendFPref : kMonahanPref;
+    S.dfpref = p.kernel == SPH_KERNEL_WENDLAND ? kWendDFPref : kMonahanPref;
+    S.overshoot = 0.f;
+    S.tol = (float)(std::max(S.L[0], S.L[1]) * 4.0e-7);
+    return S;
+}
+
+void destroy_graphs(sph_handle *h) {
+    if (h->g_step) cudaGraphExecDestroy(h->g_step);
+    if (h->g_init) cudaGraphExecDestroy(h->g_init);
+    if (h->g_forces) cudaGraphExecDestroy(h->g_forces);
+    if (h->g_prof) cudaGraphExecDestroy(h->g_prof);
+    h->g_step = h->g_init = h->g_forces = h->g_prof = nullptr;
+}
+
+// One force evaluation (plus the integration when `integrate`); with
+// `events`, an event is recorded before each stage and after the last.
+void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) {
+    Ctx c = h->ctx();
+    Launch L = h->launch();
+    auto mark = [&](int i) {
+        if (events) cudaEventRecord(h->ev[i], h->stream);
+    };
+    mark(0);
+    launch_prep(c, L, h->any_open);
+    if (h->any_open) {
+        launch_bbox(c, L, h->A, pred);
+        launch_grid(c, L);
+    }
+    launch_bin(c, L, h->A, h->T, pred);
+    mark(1);
+    launch_scan(c, L, h->T);
+    mark(2);
+    launch_permute(c, L, h->A, h->B, h->T, pred, h->mode == MODE_MIXED);
+    mark(3);
+    launch_knn(c, L, h->B, h->D, h->T, h->mode, h->tune);
+    mark(4);
+    launch_force(c, L, h->B, h->A, h->D, h->mode, integrate);
+    mark(5);
+}
+
+int count_kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return 0;
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(g, nodes.data(), &n);
+    int k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+    }
+    return k;
+}
+
+int capture(sph_handle *h, int pred, bool integrate, cudaGraphExec_t *out, bool events = false,
+            int *kernels = nullptr) {
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_eval(h, pred, integrate, events);
+    CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+    if (kernels) *kernels = count_kernel_nodes(g);
+    cudaError_t e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return SPH_OK;
+}
+
+int check_flags(sph_handle *h) {
+    unsigned f = 0;
+    CUDA_TRY(cudaMemcpyAsync(&f, h->d_flags, sizeof f, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (!f) return SPH_OK;
+    CUDA_TRY(cudaMemsetAsync(h->d_flags, 0, sizeof(unsigned), h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (f & FLAG_SENTINEL)
+        return fail(SPH_ERR_SENTINEL, "a k-th neighbour lies at squared distance >= 0.4, beyond the reference's queue sentinel");
+    if (f & FLAG_KNN_FEW) return fail(SPH_ERR_KNN, "fewer than k neighbour candidates exist for some particle");
+    if (f & FLAG_KNN_ATTEMPTS) return fail(SPH_ERR_KNN, "neighbour search radius did not converge");
+    if (f & FLAG_NONFINITE) return fail(SPH_ERR_RANGE, "non-finite particle position");
+    return fail(SPH_ERR_RANGE, "kernel argument q outside [0,1] or non-finite force");
+}
+
+int ensure_graphs(sph_handle *h) {
+    int rc;
+    if (!h->g_step && (rc = capture(h, PRED_DRIFT, true, &h->g_step, false, &h->kernels_per_step))) return rc;
+    if (!h->g_init && (rc = capture(h, PRED_INIT, false, &h->g_init))) return rc;
+    if (!h->g_forces && (rc = capture(h, PRED_KEEP, false, &h->g_forces))) return rc;
+    return SPH_OK;
+}
+
+struct Guard {
+    sph_handle *h;
+    std::lock_guard<std::mutex> lk;
+    explicit Guard(sph_handle *hh) : h(hh), lk(hh->mu) { cudaSetDevice(hh->device); }
+};
+
+int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, sph_handle **out) {
+    if (!out) return fail(SPH_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    if (!params || !counts || nsims < 1) return fail(SPH_ERR_ARG, "need at least one simulation");
+    int64_t total = 0;
+    for (int s = 0; s < nsims; s++) {
+        int rc = check_params(params[s], counts[s]);
+        if (rc) return rc;
+        if (params[s].k != params[0].k || params[s].precision != params[0].precision)
+            return fail(SPH_ERR_ARG, "k and precision must agree across an ensemble");
+        total += counts[s];
+    }
+    if (total >= kMaxParticles) return fail(SPH_ERR_ARG, "too many particles (limit 2^27)");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail(SPH_ERR_CUDA, "no CUDA device available");
+    }
+    sph_handle *h = new sph_handle();
+    cudaGetDevice(&h->device);
+    cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
+    h->nsims = nsims;
+    h->n = total;
+    h->k = params[0].k;
+    h->mode = params[0].precision == SPH_PREC_MIXED       ? MODE_MIXED
+              : params[0].precision == SPH_PREC_FP64_FAST ? MODE_FAST64
+                                                          : MODE_EXACT64;
+    h->params.assign(params, params + nsims);
+    h->offs.resize(nsims + 1);
+    h->offs[0] = 0;
+    int64_t cells = 0;
+    for (int s = 0; s < nsims; s++) {
+        h->offs[s + 1] = h->offs[s] + counts[s];
+        int level = params[s].grid_level > 0 ? params[s].grid_level : auto_level(counts[s]);
+        h->hsims.push_back(make_simdev(params[s], h->offs[s], counts[s], cells, level));
+        h->any_open = h->any_open || !h->hsims.back().periodic[0] || !h->hsims.back().periodic[1];
+        cells += (int64_t)1 << (2 * level);
+    }
+    if (cells >= ((int64_t)1 << 31) - 1) {
+        delete h;
+        return fail(SPH_ERR_ARG, "cell tables exceed 2^31 cells; lower grid_level");
+    }
+    int rc = 0;
+    auto bail = [&](int code) {
+        std::string m = g_err;
+        sph_destroy(h);
+        g_err = m;
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(SPH_ERR_CUDA, "cudaStreamCreate failed"));
+    const bool mixed = h->mode == MODE_MIXED;
+    const int64_t n = h->n, k = h->k;
+    rc |= dalloc(h, &h->d_sims, nsims);
+    rc |= dalloc(h, &h->d_offs, nsims + 1);
+    rc |= dalloc(h, &h->d_flags, 1);
+    if (rc) return bail(SPH_ERR_NOMEM);
+    if (alloc_parrays(h, h->A, mixed) || alloc_parrays(h, h->B, mixed)) return bail(SPH_ERR_NOMEM);
+    rc |= dalloc(h, &h->D.rho, n);
+    rc |= dalloc(h, &h->D.c, n);
+    rc |= dalloc(h, &h->D.h, n);
+    rc |= dalloc(h, &h->D.nbr, n * k);
+    if (mixed) {
+        rc |= dalloc(h, &h->D.derf, n);
+    } else {
+        rc |= dalloc(h, &h->D.der, n);
+        rc |= dalloc(h, &h->D.dist, n * k);
+    }
+    h->T.ncells = cells;
+    rc |= dalloc(h, &h->T.key, n);
+    rc |= dalloc(h, &h->T.rank, n);
+    rc |= dalloc(h, &h->T.count, cells);
+    rc |= dalloc(h, &h->T.start, cells + 1);
+    rc |= dalloc(h, &h->T.partial, cells / 4096 + 2);
+    h->io_doubles = (size_t)std::max<int64_t>(8 * n, 3 * n + 512);
+    rc |= dalloc(h, &h->d_io, h->io_doubles);
+    if (rc) return bail(SPH_ERR_NOMEM);
+    if (cudaMemset(h->T.count, 0, cells * sizeof(int32_t)) != cudaSuccess ||
+        cudaMemset(h->D.nbr, 0, n * k * sizeof(int32_t)) != cudaSuccess ||
+        cudaMemset(h->B.id, 0, n * sizeof(int32_t)) != cudaSuccess ||
+        cudaMemset(h->A.id, 0, n * sizeof(int32_t)) != cudaSuccess ||
+        cudaMemset(h->d_flags, 0, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(h->A.hprev, 0, n * sizeof(float)) != cudaSuccess ||
+        cudaMemcpy(h->d_sims, h->hsims.data(), nsims * sizeof(SimDev), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->d_offs, h->offs.data(), (nsims + 1) * sizeof(int64_t), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(SPH_ERR_CUDA, "device initialisation failed"));
+    knn_init_attrs();
+    h->tune.block = k > 48 ? 64 : 128;
+    h->tune.cap = (int)(k + std::max<int64_t>(16, k / 2));
+    h->tune.theta = 0.5f;
+    h->tune.hgrow = 1.04f;
+    h->tune.blocks_per_sm = std::max(1, knn_occupancy_blocks(h->tune.block, h->tune.cap, h->mode));
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return bail(fail(SPH_ERR_CUDA, cudaGetErrorString(e)));
+    *out = h;
+    return SPH_OK;
+}
+
+int copy_in(sph_handle *h, double *dst, const double *src) {
+    if (!src) return SPH_OK;
+    CUDA_TRY(cudaMemcpyAsync(dst, src, h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    return SPH_OK;
+}
+int copy_out(sph_handle *h, double *dst, const double *src) {
+    if (!dst) return SPH_OK;
+    CUDA_TRY(cudaMemcpyAsync(dst, src, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return SPH_OK;
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+extern "C" {
+
+sph_params sph_default_params(void) {
+    sph_params p;
+    memset(&p, 0, sizeof p);
+    p.k = 32;
+    p.kernel = SPH_KERNEL_MONAHAN;
+    p.precision = SPH_PREC_FP64;
+    p.grid_level = 0;
+    p.gamma = 1.66666;
+    p.mass = 1.0;
+    p.dth = 0.001;
+    p.hor[0] = -DBL_MAX;
+    p.hor[1] = DBL_MAX;
+    p.vert[0] = -DBL_MAX;
+    p.vert[1] = DBL_MAX;
+    p.refl[0] = -DBL_MAX;
+    p.refl[1] = DBL_MAX;
+    p.refl[2] = -DBL_MAX;
+    p.refl[3] = DBL_MAX;
+    p.alpha = 0.75;
+    p.beta = 1.5;
+    p.etasq = 0.01;
+    return p;
+}
+
+int32_t sph_abi_version(void) { return SPHGPU_ABI_VERSION; }
+
+const char *sph_last_error(void) { return g_err.c_str(); }
+
+int sph_device_count(int32_t *count) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (count) *count = 0;
+        return fail(SPH_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (count) *count = n;
+    return SPH_OK;
+}
+
+int sph_create(const sph_params *p, int64_t n, sph_handle **out) { return create_impl(p, &n, 1, out); }
+
+int sph_ens_create(const sph_params *params, const int64_t *counts, int32_t nsims, sph_handle **out) {
+    return create_impl(params, counts, nsims, out);
+}
+
+int sph_destroy(sph_handle *h) {
+    if (!h) return SPH_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    destroy_graphs(h);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->d_nbr_io) cudaFree(h->d_nbr_io);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return SPH_OK;
+}
+
+int sph_upload(sph_handle *h, const double *x, const double *y, const double *vx, const double *vy,
+               const double *u) {
+    if (!h || !x || !y) return fail(SPH_ERR_ARG, "handle, x and y are required");
+    Guard g(h);
+    const int64_t n = h->n;
+    double *d = h->d_io;
+    int rc;
+    if ((rc = copy_in(h, d, x)) || (rc = copy_in(h, d + n, y)) || (rc = copy_in(h, d + 2 * n, vx)) ||
+        (rc = copy_in(h, d + 3 * n, vy)) || (rc = copy_in(h, d + 4 * n, u)))
+        return rc;
+    launch_scatter_state(h->ctx(), h->launch(), h->A, d, d + n, vx ? d + 2 * n : nullptr,
+                         vy ? d + 3 * n : nullptr, u ? d + 4 * n : nullptr, nullptr, nullptr, nullptr, false);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->step = 0;
+    h->uploaded = true;
+    h->evaluated = false;
+    return SPH_OK;
+}
+
+int sph_set_state(sph_handle *h, const double *x, const double *y, const double *vx, const double *vy,
+                  const double *u, const double *ax, const double *ay, const double *udot) {
+    if (!h || !x || !y) return fail(SPH_ERR_ARG, "handle, x and y are required");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_set_state before sph_upload");
+    const int64_t n = h->n;
+    double *d = h->d_io;
+    const double *src[8] = {x, y, vx, vy, u, ax, ay, udot};
+    for (int i = 0; i < 8; i++) {
+        int rc = copy_in(h, d + i * n, src[i]);
+        if (rc) return rc;
+    }
+    launch_scatter_state(h->ctx(), h->launch(), h->A, d, d + n, vx ? d + 2 * n : nullptr,
+                         vy ? d + 3 * n : nullptr, u ? d + 4 * n : nullptr, ax ? d + 5 * n : nullptr,
+                         ay ? d + 6 * n : nullptr, udot ? d + 7 * n : nullptr, true);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_get_state(sph_handle *h, double *x, double *y, double *vx, double *vy, double *u, double *ax,
+                  double *ay, double *udot) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "no state uploaded");
+    const int64_t n = h->n;
+    double *d = h->d_io;
+    launch_gather_state(h->ctx(), h->launch(), h->A, x ? d : nullptr, y ? d + n : nullptr,
+                        vx ? d + 2 * n : nullptr, vy ? d + 3 * n : nullptr, u ? d + 4 * n : nullptr,
+                        ax ? d + 5 * n : nullptr, ay ? d + 6 * n : nullptr, udot ? d + 7 * n : nullptr);
+    CUDA_TRY(cudaGetLastError());
+    double *dst[8] = {x, y, vx, vy, u, ax, ay, udot};
+    for (int i = 0; i < 8; i++) {
+        int rc = copy_out(h, dst[i], d + i * n);
+        if (rc) return rc;
+    }
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_get_derived(sph_handle *h, double *rho, double *c, double *hsml) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "no state uploaded");
+    const int64_t n = h->n;
+    double *d = h->d_io;
+    launch_gather_derived(h->ctx(), h->launch(), h->A, h->D, rho ? d : nullptr, c ? d + n : nullptr,
+                          hsml ? d + 2 * n : nullptr);
+    CUDA_TRY(cudaGetLastError());
+    int rc;
+    if ((rc = copy_out(h, rho, d)) || (rc = copy_out(h, c, d + n)) || (rc = copy_out(h, hsml, d + 2 * n)))
+        return rc;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_get_neighbours(sph_handle *h, int64_t *ids, double *dist, int32_t *img) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (!h->uploaded || !h->evaluated) return fail(SPH_ERR_STATE, "no force evaluation yet");
+    const int64_t nk = h->n * h->k;
+    if (!h->d_nbr_io) CUDA_TRY(cudaMalloc(&h->d_nbr_io, nk * (8 + 8 + 4)));
+    int64_t *di = (int64_t *)h->d_nbr_io;
+    double *dd = (double *)(di + nk);
+    int32_t *dm = (int32_t *)(dd + nk);
+    launch_gather_neighbours(h->ctx(), h->launch(), h->A, h->B, h->D, ids ? di : nullptr,
+                             dist ? dd : nullptr, img ? dm : nullptr);
+    CUDA_TRY(cudaGetLastError());
+    if (ids) CUDA_TRY(cudaMemcpyAsync(ids, di, nk * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (dist) CUDA_TRY(cudaMemcpyAsync(dist, dd, nk * 8, cudaMemcpyDeviceToHost, h->stream));
+    if (img) CUDA_TRY(cudaMemcpyAsync(img, dm, nk * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_step(sph_handle *h, int32_t nsteps) {
+    if (!h || nsteps < 0) return fail(SPH_ERR_ARG, "bad handle or step count");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_step before sph_upload");
+    int rc = ensure_graphs(h);
+    if (rc) return rc;
+    for (int32_t s = 0; s < nsteps; s++) {
+        if (h->step == 0) CUDA_TRY(cudaGraphLaunch(h->g_init, h->stream));
+        CUDA_TRY(cudaGraphLaunch(h->g_step, h->stream));
+        h->step++;
+    }
+    if (nsteps > 0) h->evaluated = true;
+    return check_flags(h);
+}
+
+int sph_forces(sph_handle *h) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_forces before sph_upload");
+    int rc = ensure_graphs(h);
+    if (rc) return rc;
+    CUDA_TRY(cudaGraphLaunch(h->g_forces, h->stream));
+    h->evaluated = true;
+    return check_flags(h);
+}
+
+int sph_synchronize(sph_handle *h) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_host_register(void *ptr, int64_t bytes) {
+    if (!ptr || bytes <= 0) return fail(SPH_ERR_ARG, "bad pointer or size");
+    CUDA_TRY(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    return SPH_OK;
+}
+
+int sph_host_unregister(void *ptr) {
+    if (!ptr) return fail(SPH_ERR_ARG, "bad pointer");
+    CUDA_TRY(cudaHostUnregister(ptr));
+    return SPH_OK;
+}
+
+int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms) {
+    if (!h || nsteps < 0 || !ms) return fail(SPH_ERR_ARG, "bad argument");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_step_timed before sph_upload");
+    int rc = ensure_graphs(h);
+    if (rc) return rc;
+    if (!h->ev[0])
+        for (auto &e : h->ev) CUDA_TRY(cudaEventCreate(&e));
+    CUDA_TRY(cudaEventRecord(h->ev[0], h->stream));
+    for (int32_t s = 0; s < nsteps; s++) {
+        if (h->step == 0) CUDA_TRY(cudaGraphLaunch(h->g_init, h->stream));
+        CUDA_TRY(cudaGraphLaunch(h->g_step, h->stream));
+        h->step++;
+    }
+    CUDA_TRY(cudaEventRecord(h->ev[SPH_NUM_STAGES], h->stream));
+    CUDA_TRY(cudaEventSynchronize(h->ev[SPH_NUM_STAGES]));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, h->ev[0], h->ev[SPH_NUM_STAGES]));
+    *ms = t;
+    if (nsteps > 0) h->evaluated = true;
+    return check_flags(h);
+}
+
+int sph_step_profiled(sph_handle *h, int32_t nsteps, double stage_ms[SPH_NUM_STAGES]) {
+    if (!h || nsteps < 1 || !stage_ms) return fail(SPH_ERR_ARG, "bad argument");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_step_profiled before sph_upload");
+    int rc = ensure_graphs(h);
+    if (rc) return rc;
+    if (!h->ev[0])
+        for (auto &e : h->ev) CUDA_TRY(cudaEventCreate(&e));
+    if (!h->g_prof && (rc = capture(h, PRED_DRIFT, true, &h->g_prof, true))) return rc;
+    for (int i = 0; i < SPH_NUM_STAGES; i++) stage_ms[i] = 0.0;
+    for (int32_t s = 0; s < nsteps; s++) {
+        if (h->step == 0) CUDA_TRY(cudaGraphLaunch(h->g_init, h->stream));
+        CUDA_TRY(cudaGraphLaunch(h->g_prof, h->stream));
+        h->step++;
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        for (int i = 0; i < SPH_NUM_STAGES; i++) {
+            float t = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&t, h->ev[i], h->ev[i + 1]));
+            stage_ms[i] += t / nsteps;
+        }
+    }
+    h->evaluated = true;
+    return check_flags(h);
+}
+
+int32_t sph_kernels_per_step(sph_handle *h) {
+    if (!h) return -1;
+    Guard g(h);
+    if (!h->g_step && ensure_graphs(h)) return -1;
+    return h->kernels_per_step;
+}
+
+int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return fail(SPH_ERR_CUDA, "no CUDA device available");
+    }
+    if (probe_peaks(fp64_tflops, fp32_tflops)) return fail(SPH_ERR_CUDA, "throughput probe failed");
+    return SPH_OK;
+}
+
+int32_t sph_current_step(const sph_handle *h) { return h ? h->step : -1; }
+int64_t sph_num_particles(const sph_handle *h) { return h ? h->n : -1; }
+
+int sph_diagnostics(sph_handle *h, int32_t sim, double out[4]) {
+    if (!h || !out) return fail(SPH_ERR_ARG, "null argument");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "no state uploaded");
+    if (sim >= h->nsims) return fail(SPH_ERR_ARG, "simulation index out of range");
+    int64_t lo = sim < 0 ? 0 : h->offs[sim], hi = sim < 0 ? h->n : h->offs[sim + 1];
+    launch_diagnostics(h->ctx(), h->launch(), h->A, h->D, lo, hi, h->d_io);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(out, h->d_io + 3 * h->n + 3 * 64, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+}  // extern "C"

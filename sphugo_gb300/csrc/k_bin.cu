@@ -1,0 +1,240 @@
+// k_bin.cu -- cell binning: the GB300 replacement of the reference's spatial
+// index (sim/core.go:126-224 Partition/Treebuild, rebuilt on every force
+// evaluation at sim/sph.go:406). Instead of a pointer tree it builds, per
+// simulation, a dense Morton-ordered cell table at a fine level: drift +
+// cell key + histogram (one atomic per particle, whose return value is the
+// particle's rank inside its cell), an exclusive scan of the histogram into
+// cell starts, and a permute of the state into cell order. Every coarser
+// level's cell is a contiguous range of the same table, which is what the
+// neighbour search walks. All four passes are HBM streams.
+#include "common.cuh"
+
+namespace sphgpu {
+
+// ------------------------------------------------------------------ prep
+// Per-simulation reset of the per-binning reductions (one thread per sim).
+__global__ void k_prep(Ctx c) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= c.nsims) return;
+    SimDev &S = c.sims_rw[s];
+    S.overshoot = 0.f;
+    S.bbox[0] = ~0ull; S.bbox[1] = 0ull;
+    S.bbox[2] = ~0ull; S.bbox[3] = 0ull;
+}
+
+void launch_prep(const Ctx &c, const Launch &L, bool) {
+    k_prep<<<(c.nsims + 127) / 128, 128, 0, L.stream>>>(c);
+}
+
+// ------------------------------------------------------------------ bbox
+// Bounding box of the predicted positions, for simulations with an open axis.
+__global__ void k_bbox(Ctx c, PArrays A, int pred) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int s = find_sim(c.offs, c.nsims, i);
+        const SimDev &S = c.sims[s];
+        if (S.periodic[0] && S.periodic[1]) continue;
+        double2 p, vp;
+        double up;
+        predict(S, pred, A.pos[i], A.vel[i], A.acc[i], A.u[i], A.udot[i], A.vp[i], A.up[i], p, vp, up);
+        SimDev &W = c.sims_rw[s];
+        if (!S.periodic[0]) { atomicMin(&W.bbox[0], dkey(p.x)); atomicMax(&W.bbox[1], dkey(p.x)); }
+        if (!S.periodic[1]) { atomicMin(&W.bbox[2], dkey(p.y)); atomicMax(&W.bbox[3], dkey(p.y)); }
+    }
+}
+
+void launch_bbox(const Ctx &c, const Launch &L, const PArrays &A, int pred) {
+    k_bbox<<<L.sms * 4, 256, 0, L.stream>>>(c, A, pred);
+}
+
+// Grid of open axes from the bounding box (one thread per sim).
+__global__ void k_grid(Ctx c) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= c.nsims) return;
+    SimDev &S = c.sims_rw[s];
+    int G = 1 << S.level;
+    for (int ax = 0; ax < 2; ax++) {
+        if (S.periodic[ax]) continue;
+        double mn = dkey_inv(S.bbox[2 * ax]), mx = dkey_inv(S.bbox[2 * ax + 1]);
+        if (!(mn <= mx)) { mn = 0; mx = 1; }
+        double w = mx - mn;
+        if (!(w > 0)) w = 1e-300 + fabs(mn) * 1e-12 + 1e-12;
+        double L = w * (1.0 + 1e-9) + 1e-300;
+        S.lo[ax] = mn;
+        S.L[ax] = L;
+        S.s[ax] = L / G;
+        S.inv_s[ax] = G / L;
+    }
+    double Lm = fmax(S.L[0], S.L[1]);
+    S.tol = (float)(Lm * 4.0e-7);
+}
+
+void launch_grid(const Ctx &c, const Launch &L) {
+    k_grid<<<(c.nsims + 127) / 128, 128, 0, L.stream>>>(c);
+}
+
+// ------------------------------------------------------------------- bin
+__global__ void k_bin(Ctx c, PArrays A, Tables T, int pred) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int s = find_sim(c.offs, c.nsims, i);
+        const SimDev &S = c.sims[s];
+        double2 p, vp;
+        double up;
+        predict(S, pred, A.pos[i], A.vel[i], A.acc[i], A.u[i], A.udot[i], A.vp[i], A.up[i], p, vp, up);
+        if (!isfinite(p.x) || !isfinite(p.y)) atomicOr(c.flags, (unsigned)FLAG_NONFINITE);
+        int cx = cell_coord(S, 0, p.x), cy = cell_coord(S, 1, p.y);
+        // distance outside the periodic domain (the wrap moves at most one axis per step)
+        float o = 0.f;
+        if (S.periodic[0]) o = fmaxf(o, (float)fmax(S.lo[0] - p.x, p.x - (S.lo[0] + S.L[0])));
+        if (S.periodic[1]) o = fmaxf(o, (float)fmax(S.lo[1] - p.y, p.y - (S.lo[1] + S.L[1])));
+        if (o > 0.f) atomicMax((int *)&c.sims_rw[s].overshoot, __float_as_int(o * 1.0001f));
+        int32_t key = (int32_t)(S.cell_off + morton2(cx, cy));
+        T.key[i] = key;
+        T.rank[i] = atomicAdd(&T.count[key], 1);
+    }
+}
+
+void launch_bin(const Ctx &c, const Launch &L, const PArrays &A, const Tables &T, int pred) {
+    k_bin<<<L.sms * 8, 256, 0, L.stream>>>(c, A, T, pred);
+}
+
+// ------------------------------------------------------------------ scan
+// Exclusive scan of the cell counts into cell starts (three passes over
+// tiles of kScanTile cells), zeroing the counts for the next binning.
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &total) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        int t = lane < nw ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) warp_sums[lane] = t;
+    }
+    __syncthreads();
+    total = warp_sums[(blockDim.x >> 5) - 1];
+    int before = w > 0 ? warp_sums[w - 1] : 0;
+    int r = before + x - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_scan_tiles(Tables T) {
+    __shared__ int ws[32];
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int sum = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+        int64_t idx = base + j;
+        if (idx < T.ncells) sum += T.count[idx];
+    }
+    int total;
+    block_exclusive_scan(sum, ws, total);
+    if (threadIdx.x == 0) T.partial[blockIdx.x] = total;
+}
+
+__global__ void k_scan_partials(Tables T, int ntiles) {
+    __shared__ int ws[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b = 0; b < ntiles; b += blockDim.x) {
+        int idx = b + threadIdx.x;
+        int v = idx < ntiles ? T.partial[idx] : 0;
+        int total;
+        int ex = block_exclusive_scan(v, ws, total);
+        if (idx < ntiles) T.partial[idx] = ex + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) T.start[T.ncells] = carry;
+}
+
+__global__ void k_scan_final(Tables T) {
+    __shared__ int ws[32];
+    int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int sum = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+        int64_t idx = base + j;
+        v[j] = idx < T.ncells ? T.count[idx] : 0;
+        sum += v[j];
+    }
+    int total;
+    int ex = block_exclusive_scan(sum, ws, total) + T.partial[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+        int64_t idx = base + j;
+        if (idx < T.ncells) {
+            T.start[idx] = ex;
+            T.count[idx] = 0;
+        }
+        ex += v[j];
+    }
+}
+
+void launch_scan(const Ctx &, const Launch &L, const Tables &T) {
+    int ntiles = (int)((T.ncells + kScanTile - 1) / kScanTile);
+    k_scan_tiles<<<ntiles, kScanThreads, 0, L.stream>>>(T);
+    k_scan_partials<<<1, 1024, 0, L.stream>>>(T, ntiles);
+    k_scan_final<<<ntiles, kScanThreads, 0, L.stream>>>(T);
+}
+
+// --------------------------------------------------------------- permute
+// Writes the predicted state into cell order (B), plus the float-pair
+// position record relative to the grid origin used by the FP32 distance
+// filter and the mixed-precision sums.
+__global__ void k_permute(Ctx c, PArrays A, PArrays B, Tables T, int pred, int mixed) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        int s = find_sim(c.offs, c.nsims, i);
+        const SimDev &S = c.sims[s];
+        int64_t d = (int64_t)T.start[T.key[i]] + T.rank[i];
+        double2 pos = A.pos[i], vel = A.vel[i];
+        double u = A.u[i];
+        double2 p, vp;
+        double up;
+        predict(S, pred, pos, vel, A.acc[i], u, A.udot[i], A.vp[i], A.up[i], p, vp, up);
+        B.pos[d] = p;
+        B.vel[d] = vel;
+        B.vp[d] = vp;
+        B.u[d] = u;
+        B.up[d] = up;
+        B.id[d] = A.id[i];
+        B.hprev[d] = A.hprev[i];
+        float4 r;
+        split_df(__dsub_rn(p.x, S.lo[0]), r.x, r.z);
+        split_df(__dsub_rn(p.y, S.lo[1]), r.y, r.w);
+        B.rec[d] = r;
+        if (mixed) {
+            float4 v;
+            split_df(vp.x, v.x, v.z);
+            split_df(vp.y, v.y, v.w);
+            B.vrec[d] = v;
+        }
+    }
+}
+
+void launch_permute(const Ctx &c, const Launch &L, const PArrays &A, const PArrays &B,
+                    const Tables &T, int pred, bool mixed) {
+    k_permute<<<L.sms * 8, 256, 0, L.stream>>>(c, A, B, T, pred, mixed ? 1 : 0);
+}
+
+}  // namespace sphgpu

@@ -1,0 +1,221 @@
+// k_force.cu -- pressure + artificial-viscosity acceleration and du/dt
+// (sim/sph.go:327-401 AccelerationAndEDot2D) fused with the rest of the
+// leapfrog step (sim/sph.go:121-193: kick, drift, periodic wrap,
+// reflections). One thread per particle walks its k neighbours from the
+// farthest to the nearest, as the reference's loop does, gathering the
+// neighbours' predicted velocity, sound speed, density and smoothing length.
+#include "physics.cuh"
+
+namespace sphgpu {
+
+struct ForceArgs {
+    Ctx c;
+    PArrays B;  // positions / predictions of this evaluation (cell order)
+    PArrays A;  // state written here (same order)
+    Derived D;
+    int integrate;
+};
+
+// sim/sph.go:121-193 with two roundings per multiply-add.
+__device__ __forceinline__ void integrate_one(const SimDev &S, double2 &pos, double2 &vel, double &u,
+                                              double ax, double ay, double udot) {
+    const double dth = S.dth;
+    const double dt2 = __dmul_rn(2.0, dth);
+    vel.x = __dadd_rn(vel.x, __dmul_rn(ax, dt2));
+    vel.y = __dadd_rn(vel.y, __dmul_rn(ay, dt2));
+    u = __dadd_rn(u, __dmul_rn(__dmul_rn(udot, 2.0), dth));
+    pos.x = __dadd_rn(pos.x, __dmul_rn(vel.x, dth));
+    pos.y = __dadd_rn(pos.y, __dmul_rn(vel.y, dth));
+    // periodic wrap: an if/continue chain, at most one axis per step
+    if (pos.x < S.per_lo[0]) pos.x = __dadd_rn(pos.x, __dsub_rn(S.per_hi[0], S.per_lo[0]));
+    else if (pos.x > S.per_hi[0]) pos.x = __dsub_rn(pos.x, __dsub_rn(S.per_hi[0], S.per_lo[0]));
+    else if (pos.y < S.per_lo[1]) pos.y = __dadd_rn(pos.y, __dsub_rn(S.per_hi[1], S.per_lo[1]));
+    else if (pos.y > S.per_hi[1]) pos.y = __dsub_rn(pos.y, __dsub_rn(S.per_hi[1], S.per_lo[1]));
+    // reflections: Pos -= Pos - bound; Vel = -Vel
+    if (pos.x < S.refl[0]) { pos.x = __dsub_rn(pos.x, __dsub_rn(pos.x, S.refl[0])); vel.x = -vel.x; }
+    if (pos.x > S.refl[1]) { pos.x = __dsub_rn(pos.x, __dsub_rn(pos.x, S.refl[1])); vel.x = -vel.x; }
+    if (pos.y < S.refl[2]) { pos.y = __dsub_rn(pos.y, __dsub_rn(pos.y, S.refl[2])); vel.y = -vel.y; }
+    if (pos.y > S.refl[3]) { pos.y = __dsub_rn(pos.y, __dsub_rn(pos.y, S.refl[3])); vel.y = -vel.y; }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_force(ForceArgs a) {
+    const int k = a.c.k;
+    const PArrays &B = a.B;
+    const Derived &D = a.D;
+    unsigned fl = 0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < a.c.n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int s = find_sim(a.c.offs, a.c.nsims, q);
+        const SimDev &S = a.c.sims[s];
+        const double2 P = B.pos[q];
+        const int32_t *nb = D.nbr + q * k;
+        double axo, ayo, edot;
+        if (MODE == MODE_EXACT64) {
+            const double4 di = D.der[q];
+            const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
+            const double2 vpi = B.vp[q];
+            const double2 *dist = D.dist + q * k;
+            double ax = 0.0, ay = 0.0, ed = 0.0;
+            for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
+                const uint32_t code = (uint32_t)nb[e];
+                const uint32_t j = code >> kCodeShift;
+                const double d = dist[e].x;
+                const double qq = __ddiv_rn(d, hi);
+                if (qq > 1.0 || qq < 0.0) fl |= FLAG_Q_RANGE;
+                const double drk = kdf_exact(S.kernel, qq);
+                const double4 dj = D.der[j];
+                const double2 vpj = B.vp[j];
+                const double vabx = __dsub_rn(vpj.x, vpi.x), vaby = __dsub_rn(vpj.y, vpi.y);
+                double ox, oy;
+                img_shift(S, code & 15u, ox, oy);
+                const double2 Q = B.pos[j];
+                const double rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
+                const double raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
+                const double dot = __dadd_rn(__dmul_rn(vabx, rabx), __dmul_rn(vaby, raby));
+                double piab = 0.0;
+                if (dot < 0.0) {
+                    const double cab = __dmul_rn(0.5, __dadd_rn(ci, dj.x));
+                    const double rhoab = __dmul_rn(0.5, __dadd_rn(rhoi, dj.y));
+                    const double hab = __dmul_rn(0.5, __dadd_rn(hi, dj.z));
+                    const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
+                    const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, S.etasq));
+                    piab = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-S.alpha, cab), mu),
+                                               __dmul_rn(__dmul_rn(S.beta, mu), mu)), rhoab);
+                }
+                const double sum3 = __dadd_rn(__dadd_rn(piab, ca), dj.w);
+                ax = __dadd_rn(ax, __ddiv_rn(__dmul_rn(__dmul_rn(rabx, sum3), drk), d));
+                ay = __dadd_rn(ay, __ddiv_rn(__dmul_rn(__dmul_rn(raby, sum3), drk), d));
+                ed = __dadd_rn(ed, __dmul_rn(dot, drk));
+            }
+            const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
+            axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
+            ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
+            edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
+        } else if (MODE == MODE_FAST64) {
+            const double4 di = D.der[q];
+            const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
+            const double inv_h = 1.0 / hi;
+            const double2 vpi = B.vp[q];
+            const double2 *dist = D.dist + q * k;
+            const double alpha = S.alpha, beta = S.beta, etasq = S.etasq;
+            double ax = 0.0, ay = 0.0, ed = 0.0;
+            for (int e = k - 1; e >= 0; e--) {
+                const uint32_t code = (uint32_t)nb[e];
+                const uint32_t j = code >> kCodeShift;
+                const double2 dd = dist[e];
+                const double qq = fmin(dd.x * inv_h, 1.0);
+                const double drk = kdf_fast(S.kernel, qq);
+                const double4 dj = D.der[j];
+                const double2 vpj = B.vp[j];
+                const double vabx = vpj.x - vpi.x, vaby = vpj.y - vpi.y;
+                double ox, oy;
+                img_shift(S, code & 15u, ox, oy);
+                const double2 Q = B.pos[j];
+                const double rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
+                const double raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
+                const double dot = vabx * rabx + vaby * raby;
+                double piab = 0.0;
+                if (dot < 0.0) {
+                    const double cab = 0.5 * (ci + dj.x);
+                    const double rhoab = 0.5 * (rhoi + dj.y);
+                    const double hab = 0.5 * (hi + dj.z);
+                    const double mu = dot * hab / (rabx * rabx + raby * raby + etasq);
+                    piab = mu * (beta * mu - alpha * cab) / rhoab;
+                }
+                const double w = (piab + ca + dj.w) * drk * dd.y;
+                ax += rabx * w;
+                ay += raby * w;
+                ed += dot * drk;
+            }
+            const double f = S.mass * S.dfpref * (inv_h * inv_h * inv_h);
+            axo = ax * f + S.accel[0];
+            ayo = ay * f + S.accel[1];
+            edot = ca * ed * S.mass;
+        } else {
+            const float4 di = D.derf[q];
+            const double hi = D.h[q];
+            const double ca = D.c[q] * D.c[q] / (S.gamma * D.rho[q]);
+            const float ci = di.x, rhoi = di.y, hif = di.z, caf = di.w;
+            const float inv_hf = 1.f / hif;
+            const float4 pr = B.rec[q];
+            const float4 vi = B.vrec[q];
+            const float alpha = (float)S.alpha, beta = (float)S.beta, etasq = (float)S.etasq;
+            const float dXh = __double2float_rn(S.dimg[0]);
+            const float dXl = __double2float_rn(S.dimg[0] - (double)dXh);
+            const float dYh = __double2float_rn(S.dimg[1]);
+            const float dYl = __double2float_rn(S.dimg[1] - (double)dYh);
+            KahanF ax, ay, ed;
+            for (int e = k - 1; e >= 0; e--) {
+                const uint32_t code = (uint32_t)nb[e];
+                const uint32_t j = code >> kCodeShift;
+                const uint32_t img = code & 15u;
+                const int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
+                const float4 r = __ldg(&B.rec[j]);
+                // r_AB = (q - offset) - p from float pairs (see the kNN kernel)
+                const float rabx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
+                                   (r.z - (pr.z + (float)ia * dXl));
+                const float raby = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
+                                   (r.w - (pr.w + (float)ib * dYl));
+                const float d2 = __fmaf_rn(rabx, rabx, raby * raby);
+                const float invd = rsqrtf(d2);
+                const float qq = fminf(d2 * invd * inv_hf, 1.f);
+                const float drk = kdf_f32(S.kernel, qq);
+                const float4 vj = __ldg(&B.vrec[j]);
+                const float4 dj = __ldg(&D.derf[j]);
+                const float vabx = (vj.x - vi.x) + (vj.z - vi.z);
+                const float vaby = (vj.y - vi.y) + (vj.w - vi.w);
+                const float dot = vabx * rabx + vaby * raby;
+                float piab = 0.f;
+                if (dot < 0.f) {
+                    const float cab = 0.5f * (ci + dj.x);
+                    const float rhoab = 0.5f * (rhoi + dj.y);
+                    const float hab = 0.5f * (hif + dj.z);
+                    const float mu = dot * hab / (d2 + etasq);
+                    piab = mu * (beta * mu - alpha * cab) / rhoab;
+                }
+                const float w = (piab + caf + dj.w) * drk * invd;
+                ax.add(rabx * w);
+                ay.add(raby * w);
+                ed.add(dot * drk);
+            }
+            const double f = S.mass * S.dfpref / (hi * hi * hi);
+            axo = ax.value() * f + S.accel[0];
+            ayo = ay.value() * f + S.accel[1];
+            edot = ca * ed.value() * S.mass;
+        }
+        if (!isfinite(axo) || !isfinite(ayo) || !isfinite(edot)) fl |= FLAG_Q_RANGE;
+        double2 pos = P, vel = B.vel[q];
+        double u = B.u[q];
+        if (a.integrate) integrate_one(S, pos, vel, u, axo, ayo, edot);
+        a.A.pos[q] = pos;
+        a.A.vel[q] = vel;
+        a.A.u[q] = u;
+        a.A.acc[q] = make_double2(axo, ayo);
+        a.A.udot[q] = edot;
+        a.A.id[q] = B.id[q];
+        a.A.hprev[q] = (float)D.h[q];
+        a.A.vp[q] = B.vp[q];
+        a.A.up[q] = B.up[q];
+    }
+    if (fl) atomicOr(a.c.flags, fl);
+}
+
+void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays &A,
+                  const Derived &D, int mode, bool integrate) {
+    ForceArgs a;
+    a.c = c;
+    a.B = B;
+    a.A = A;
+    a.D = D;
+    a.integrate = integrate ? 1 : 0;
+    const int block = 128;
+    int64_t need = (c.n + block - 1) / block;
+    int grid = (int)(need < (int64_t)L.sms * 16 ? need : (int64_t)L.sms * 16);
+    if (grid < 1) grid = 1;
+    if (mode == MODE_EXACT64) k_force<MODE_EXACT64><<<grid, block, 0, L.stream>>>(a);
+    else if (mode == MODE_FAST64) k_force<MODE_FAST64><<<grid, block, 0, L.stream>>>(a);
+    else k_force<MODE_MIXED><<<grid, block, 0, L.stream>>>(a);
+}
+
+}  // namespace sphgpu

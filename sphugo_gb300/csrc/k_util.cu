@@ -1,0 +1,242 @@
+// k_util.cu -- state transfer between the caller's particle order and the
+// cell order kept on the device, neighbour-list export in the reference's
+// layout, and the diagnostics of sim/sph.go:441-463.
+#include "physics.cuh"
+
+namespace sphgpu {
+
+#define GRID_STRIDE(i, n) \
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+static int grid_for(const Launch &L, int64_t n, int block) {
+    int64_t need = (n + block - 1) / block;
+    int64_t cap = (int64_t)L.sms * 16;
+    int g = (int)(need < cap ? need : cap);
+    return g < 1 ? 1 : g;
+}
+
+__global__ void k_gather_state(Ctx c, PArrays A, double *x, double *y, double *vx, double *vy,
+                               double *u, double *ax, double *ay, double *udot) {
+    GRID_STRIDE(i, c.n) {
+        int32_t id = A.id[i];
+        double2 p = A.pos[i], v = A.vel[i], a = A.acc[i];
+        if (x) x[id] = p.x;
+        if (y) y[id] = p.y;
+        if (vx) vx[id] = v.x;
+        if (vy) vy[id] = v.y;
+        if (u) u[id] = A.u[i];
+        if (ax) ax[id] = a.x;
+        if (ay) ay[id] = a.y;
+        if (udot) udot[id] = A.udot[i];
+    }
+}
+
+void launch_gather_state(const Ctx &c, const Launch &L, const PArrays &A, double *x, double *y,
+                         double *vx, double *vy, double *u, double *ax, double *ay, double *udot) {
+    k_gather_state<<<grid_for(L, c.n, 256), 256, 0, L.stream>>>(c, A, x, y, vx, vy, u, ax, ay, udot);
+}
+
+// have_acc = 0: fresh upload, slot i holds particle i and the integrator
+// history (accelerations, predictions, radius guess) starts from zero.
+// have_acc = 1: replace the state of every particle in its current slot.
+__global__ void k_scatter_state(Ctx c, PArrays A, const double *x, const double *y, const double *vx,
+                                const double *vy, const double *u, const double *ax, const double *ay,
+                                const double *udot, int have_acc) {
+    GRID_STRIDE(i, c.n) {
+        int32_t id;
+        if (have_acc) {
+            id = A.id[i];
+        } else {
+            id = (int32_t)i;
+            A.id[i] = id;
+            A.hprev[i] = 0.f;
+        }
+        double2 v = make_double2(vx ? vx[id] : 0.0, vy ? vy[id] : 0.0);
+        double e = u ? u[id] : 0.0;
+        A.pos[i] = make_double2(x[id], y[id]);
+        A.vel[i] = v;
+        A.u[i] = e;
+        if (have_acc) {
+            A.acc[i] = make_double2(ax ? ax[id] : 0.0, ay ? ay[id] : 0.0);
+            A.udot[i] = udot ? udot[id] : 0.0;
+        } else {
+            A.acc[i] = make_double2(0.0, 0.0);
+            A.udot[i] = 0.0;
+        }
+        A.vp[i] = v;
+        A.up[i] = e;
+    }
+}
+
+void launch_scatter_state(const Ctx &c, const Launch &L, const PArrays &A, const double *x,
+                          const double *y, const double *vx, const double *vy, const double *u,
+                          const double *ax, const double *ay, const double *udot, bool have_acc) {
+    k_scatter_state<<<grid_for(L, c.n, 256), 256, 0, L.stream>>>(c, A, x, y, vx, vy, u, ax, ay, udot,
+                                                                 have_acc ? 1 : 0);
+}
+
+__global__ void k_gather_derived(Ctx c, PArrays A, Derived D, double *rho, double *cs, double *h) {
+    GRID_STRIDE(i, c.n) {
+        int32_t id = A.id[i];
+        if (rho) rho[id] = D.rho[i];
+        if (cs) cs[id] = D.c[i];
+        if (h) h[id] = D.h[i];
+    }
+}
+
+void launch_gather_derived(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D,
+                           double *rho, double *cs, double *h) {
+    k_gather_derived<<<grid_for(L, c.n, 256), 256, 0, L.stream>>>(c, A, D, rho, cs, h);
+}
+
+// Reference layout: slot 0 = farthest (sim/nearest-neighbour.go:139-153 keeps
+// NNDists descending). dist = sqrt of the reference's squared distance.
+__global__ void k_gather_nbrs(Ctx c, PArrays B, Derived D, int have_dist, int64_t *ids, double *dist,
+                              int32_t *img) {
+    const int k = c.k;
+    GRID_STRIDE(i, c.n) {
+        const int s = find_sim(c.offs, c.nsims, i);
+        const SimDev &S = c.sims[s];
+        const int64_t idq = B.id[i];
+        const double2 P = B.pos[i];
+        for (int e = 0; e < k; e++) {
+            uint32_t code = (uint32_t)D.nbr[i * k + e];
+            uint32_t j = code >> kCodeShift;
+            int64_t o = idq * k + (k - 1 - e);
+            if (ids) ids[o] = B.id[j];
+            if (img) img[o] = (int32_t)(code & 15u);
+            if (dist) {
+                if (have_dist) {
+                    dist[o] = D.dist[i * k + e].x;
+                } else {
+                    double ox, oy;
+                    img_shift(S, code & 15u, ox, oy);
+                    double2 Q = B.pos[j];
+                    dist[o] = __dsqrt_rn(dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y));
+                }
+            }
+        }
+    }
+}
+
+void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &, const PArrays &B,
+                              const Derived &D, int64_t *ids, double *dist, int32_t *img) {
+    k_gather_nbrs<<<grid_for(L, c.n, 128), 128, 0, L.stream>>>(c, B, D, D.dist ? 1 : 0, ids, dist, img);
+}
+
+// ---- diagnostics: deterministic sums over the caller's particle order.
+// scratch layout: e[n], r[n], v[n] in id order, then block partials.
+constexpr int kRedBlock = 256;
+
+__global__ void k_diag_scatter(Ctx c, PArrays A, Derived D, double *scr) {
+    GRID_STRIDE(i, c.n) {
+        int32_t id = A.id[i];
+        double2 v = A.vel[i];
+        scr[id] = A.u[i];
+        scr[c.n + id] = D.rho[i];
+        // Vec2.Norm (sim/linear-algebra.go:54-56): sqrt(x*x + y*y), two roundings
+        scr[2 * c.n + id] = __dsqrt_rn(__dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)));
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) r += sh[i];
+    __syncthreads();
+    return r;
+}
+
+// one block per (quantity, chunk); fixed chunking makes the sum order fixed
+__global__ void k_diag_reduce(const double *scr, int64_t n, int64_t lo, int64_t hi, double *part) {
+    __shared__ double sh[32];
+    const int qn = blockIdx.y;
+    const int64_t chunk = (hi - lo + gridDim.x - 1) / gridDim.x;
+    const int64_t b0 = lo + blockIdx.x * chunk, b1 = min(hi, b0 + chunk);
+    double v = 0.0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) v += scr[qn * n + i];
+    double r = block_sum(v, sh);
+    if (threadIdx.x == 0) part[qn * gridDim.x + blockIdx.x] = r;
+}
+
+__global__ void k_diag_final(const double *scr, int64_t n, int64_t hi, const double *part, int nb,
+                             double *out4) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < 3; q++)
+        for (int b = 0; b < nb; b++) s[q] += part[q * nb + b];
+    out4[0] = s[0];
+    out4[1] = s[1];
+    out4[2] = hi > 0 ? scr[2 * n + hi - 1] : 0.0;  // the reference's assignment: last particle only
+    out4[3] = s[2];
+}
+
+void launch_diagnostics(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D, int64_t lo,
+                        int64_t hi, double *scratch) {
+    // scratch: 3n doubles in id order, 3*nb block partials, then 4 outputs
+    const int nb = 64;
+    double *part = scratch + 3 * c.n;
+    double *out4 = part + 3 * nb;
+    k_diag_scatter<<<grid_for(L, c.n, 256), 256, 0, L.stream>>>(c, A, D, scratch);
+    dim3 g(nb, 3);
+    k_diag_reduce<<<g, kRedBlock, 0, L.stream>>>(scratch, c.n, lo, hi, part);
+    k_diag_final<<<1, 32, 0, L.stream>>>(scratch, c.n, hi, part, nb, out4);
+}
+
+// ---- arithmetic throughput probe: 8 independent FMA chains per thread
+template <typename T>
+__global__ void k_fma_chains(T *out, int iters, T a, T b) {
+    T x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = (T)(threadIdx.x * 1e-3 + i);
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = fma(x[i], a, b);
+    }
+    T s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    if (s == (T)12345.678) out[0] = s;  // keeps the chains live
+}
+
+int probe_peaks(double *fp64_tflops, double *fp32_tflops) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void *buf = nullptr;
+    if (cudaMalloc(&buf, 64) != cudaSuccess) return -1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256;
+    auto run = [&](auto kern, auto a, auto b, int iters) {
+        kern<<<blocks, threads>>>((decltype(a) *)buf, 8, a, b);
+        cudaDeviceSynchronize();
+        float best = 1e30f;
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(e0);
+            kern<<<blocks, threads>>>((decltype(a) *)buf, iters, a, b);
+            cudaEventRecord(e1);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = ms < best ? ms : best;
+        }
+        return 2.0 * blocks * threads * 8.0 * iters / (best * 1e-3) / 1e12;
+    };
+    double d = run(k_fma_chains<double>, 0.999999, 1e-7, 2000);
+    double f = run(k_fma_chains<float>, 0.999999f, 1e-7f, 20000);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    if (fp64_tflops) *fp64_tflops = d;
+    if (fp32_tflops) *fp32_tflops = f;
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace sphgpu
