@@ -246,6 +246,8 @@ def main():
     ap.add_argument("--n", type=int, default=0, help="override the particle count (testing only)")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--form", default="exact", choices=["exact", "fast", "mixed"],
+                    help="arithmetic form of the headline run (profiling only; default exact)")
     args = ap.parse_args()
     dist = Dist()
     try:
@@ -266,7 +268,8 @@ def run_ours(args, dist):
     fp64_pk, fp32_pk = C.c_double(0), C.c_double(0)
     L.check(lib.sph_probe_peaks(C.byref(fp64_pk), C.byref(fp32_pk)))
 
-    sim = make_sim(n, "Exact", SEED + 1000 * dist.rank)
+    form = {"exact": "Exact", "fast": "Fast", "mixed": "Mixed"}[args.form]
+    sim = make_sim(n, form, SEED + 1000 * dist.rank)
     sim.Step(W)
     kernels = int(lib.sph_kernels_per_step(sim._h))
     clk = ClockSampler(dist.local)

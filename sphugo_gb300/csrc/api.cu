@@ -198,7 +198,8 @@ void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) 
     Ctx c = h->ctx();
     Launch L = h->launch();
     auto mark = [&](int i) {
-        if (events) cudaEventRecord(h->ev[i], h->stream);
+        // external event nodes (plain records only order work inside a capture)
+        if (events) cudaEventRecordWithFlags(h->ev[i], h->stream, cudaEventRecordExternal);
     };
     mark(0);
     launch_prep(c, L, h->any_open);
@@ -533,7 +534,7 @@ int sph_get_neighbours(sph_handle *h, int64_t *ids, double *dist, int32_t *img) 
     double *dd = (double *)(di + nk);
     int32_t *dm = (int32_t *)(dd + nk);
     launch_gather_neighbours(h->ctx(), h->launch(), h->A, h->B, h->D, ids ? di : nullptr,
-                             dist ? dd : nullptr, img ? dm : nullptr);
+                             dist ? dd : nullptr, img ? dm : nullptr, h->mode == MODE_EXACT64);
     CUDA_TRY(cudaGetLastError());
     if (ids) CUDA_TRY(cudaMemcpyAsync(ids, di, nk * 8, cudaMemcpyDeviceToHost, h->stream));
     if (dist) CUDA_TRY(cudaMemcpyAsync(dist, dd, nk * 8, cudaMemcpyDeviceToHost, h->stream));

@@ -205,7 +205,7 @@ void launch_scatter_state(const Ctx &c, const Launch &L, const PArrays &A, const
 void launch_gather_derived(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D,
                            double *rho, double *cs, double *h);
 void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &A, const PArrays &B,
-                              const Derived &D, int64_t *ids, double *dist, int32_t *img);
+                              const Derived &D, int64_t *ids, double *dist, int32_t *img, bool exact_stored);
 void launch_diagnostics(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D,
                         int64_t lo, int64_t hi, double *scratch);
 int knn_occupancy_blocks(int block, int cap, int mode);

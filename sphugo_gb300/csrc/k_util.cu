@@ -119,9 +119,11 @@ __global__ void k_gather_nbrs(Ctx c, PArrays B, Derived D, int have_dist, int64_
     }
 }
 
+// The FP64 form stores the reference's NNDists; the others recompute them
+// from the evaluation's positions (their stored distances are approximations).
 void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &, const PArrays &B,
-                              const Derived &D, int64_t *ids, double *dist, int32_t *img) {
-    k_gather_nbrs<<<grid_for(L, c.n, 128), 128, 0, L.stream>>>(c, B, D, D.dist ? 1 : 0, ids, dist, img);
+                              const Derived &D, int64_t *ids, double *dist, int32_t *img, bool exact_stored) {
+    k_gather_nbrs<<<grid_for(L, c.n, 128), 128, 0, L.stream>>>(c, B, D, exact_stored ? 1 : 0, ids, dist, img);
 }
 
 // ---- diagnostics: deterministic sums over the caller's particle order.
