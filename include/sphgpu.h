@@ -135,6 +135,27 @@ int32_t sph_kernels_per_step(sph_handle *h);
  * in TFLOP/s (2 flops per FMA), from independent FMA chains. */
 int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops);
 
+/* ---- allocation-free neighbour search and density ----
+ * No counterpart in the reference. For callers that cannot call cudaMalloc
+ * (a host framework that owns the device memory pool, or a latency-critical
+ * loop where an allocation may synchronise the device): the exact periodic
+ * kNN and density of one small particle set (the SPH_PREC_FP64 arithmetic of
+ * a force evaluation), with every intermediate array in a static device
+ * scratch area of about 8 MB that each GPU loading this library holds until
+ * the process exits. x, y (n each) and the outputs are device-accessible
+ * pointers; any output may be NULL: nbr_ids / nbr_dist (n*k, slot 0 =
+ * farthest, as sph_get_neighbours), rho and hsml (n). stream is a
+ * cudaStream_t (NULL = the default stream); the call returns after its work
+ * on that stream is done. n <= SPH_NOALLOC_MAX_N and k <= SPH_NOALLOC_MAX_K,
+ * else SPH_ERR_ARG. The first call on a device looks up the scratch's device
+ * address and sets kernel attributes, so make it before any stream capture.
+ * All calls share the scratch: calls that overlap on the GPU (other threads
+ * or streams) race, so serialise them. p->precision is ignored. */
+#define SPH_NOALLOC_MAX_N 8192
+#define SPH_NOALLOC_MAX_K 32
+int sph_density_noalloc(const sph_params *p, const double *x, const double *y, int32_t n, int64_t *nbr_ids,
+                        double *nbr_dist, double *rho, double *hsml, void *stream);
+
 /* Page-locks (pins) caller memory so that transfers from / to it run at
  * full link speed; no reference counterpart. */
 int sph_host_register(void *ptr, int64_t bytes);

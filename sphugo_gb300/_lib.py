@@ -41,7 +41,10 @@ EXPORTS = [
     "sph_ic_stress", "sph_ic_ensemble", "sph_config_default", "sph_config_load",
     "sph_config_start_count", "sph_config_spawn", "sph_point_source_spawn",
     "sph_step_timed", "sph_step_profiled", "sph_kernels_per_step", "sph_probe_peaks",
+    "sph_density_noalloc",
 ]
+NOALLOC_MAX_N = 8192
+NOALLOC_MAX_K = 32
 NUM_STAGES = 5
 STAGES = ["bin", "scan", "permute", "knn_density", "force_integrate"]
 
@@ -139,6 +142,7 @@ def load() -> C.CDLL:
     L.sph_kernels_per_step.argtypes = [vp]
     L.sph_kernels_per_step.restype = C.c_int32
     L.sph_probe_peaks.argtypes = [dp, dp]
+    L.sph_density_noalloc.argtypes = [C.POINTER(SphParams), vp, vp, C.c_int32, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -48,6 +48,8 @@ int auto_level(int64_t n) {
 }
 }  // namespace
 
+void sphgpu::set_last_error(const std::string &msg) { g_err = msg; }
+
 struct sph_handle {
     int device = 0, sms = 0;
     cudaStream_t stream = nullptr;

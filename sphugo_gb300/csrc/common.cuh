@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/sphgpu.h"
 
 namespace sphgpu {
@@ -210,5 +212,7 @@ void launch_diagnostics(const Ctx &c, const Launch &L, const PArrays &A, const D
                         int64_t lo, int64_t hi, double *scratch);
 int knn_occupancy_blocks(int block, int cap, int mode);
 int probe_peaks(double *fp64_tflops, double *fp32_tflops);
+// message returned by sph_last_error() on this thread
+void set_last_error(const std::string &msg);
 
 }  // namespace sphgpu
