@@ -174,6 +174,44 @@ def profile(sim, steps=3):
     return dict(zip(L.STAGES, out.tolist()))
 
 
+def ensemble_case(form, steps, nsims):
+    """256 independent simulations: one graph per ensemble step vs one by one."""
+    from sphugo_gb300 import ics
+    from sphugo_gb300 import sim as S
+    confs, arrays = ics.make_ensemble(nsims=nsims, precision=form)
+    ntot = sum(len(a[0]) for a in arrays)
+    e = S.Ensemble(confs, arrays)
+    e.Step(2)
+    ms = timed(e, steps)
+    e.close()
+    sims = [S.Simulation(c, *a) for c, a in zip(confs, arrays)]
+    for s in sims:
+        s.Step(2)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s in sims:
+            s.Step(1)
+    sep = time.perf_counter() - t0
+    for s in sims:
+        s.close()
+    graph = ntot * steps / (ms / 1e3)
+    one = ntot * steps / sep
+    return {"n_total": ntot, "sims": nsims, "graph": graph, "one_by_one": one, "ratio": graph / one}
+
+
+def workload_case(kind, n, k, dt, seed, form, steps, grid_level=0):
+    from sphugo_gb300 import ics
+    from sphugo_gb300 import sim as S
+    arrs = {"clustered": ics.clustered, "stress": ics.stress}[kind](n, seed)
+    conf = ics.periodic_config(n, k, dt, form, grid_level=grid_level)
+    sim = S.Simulation(conf, *arrs)
+    sim.Step(2)
+    ms = timed(sim, steps)
+    st = profile(sim, 2)
+    sim.close()
+    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st}
+
+
 def e2e_run(sim, steps):
     """set_state from pinned host arrays + step + get_state, every step."""
     import numpy as np
@@ -322,6 +360,16 @@ def run_ours(args, dist):
                 "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3)}
             s2.close()
         extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
+        ens = {}
+        for form in ("Exact", "Mixed"):
+            ens[form.lower()] = ensemble_case(form, 5, 256)
+        extras["ensemble_256"] = ens
+        clu = {f.lower(): workload_case("clustered", 4_194_304, 32, 1e-5, 3, f, 5) for f in ("Exact", "Mixed")}
+        clu["mixed_vs_fp64"] = clu["mixed"]["value"] / clu["exact"]["value"]
+        extras["clustered_N4194304_k32"] = clu
+        stress = {f.lower(): workload_case("stress", 16_777_216, 64, 1e-6, 4, f, 3) for f in ("Exact", "Mixed")}
+        stress["mixed_vs_fp64"] = stress["mixed"]["value"] / stress["exact"]["value"]
+        extras["stress_N16777216_k64"] = stress
 
     cpu = None
     if not args.no_cpu and dist.rank == 0:

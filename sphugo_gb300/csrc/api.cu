@@ -183,6 +183,7 @@ SimDev make_simdev(const sph_params &p, int64_t off, int64_t n, int64_t cell_off
     S.dfpref = p.kernel == SPH_KERNEL_WENDLAND ? kWendDFPref : kMonahanPref;
     S.overshoot = 0.f;
     S.tol = (float)(std::max(S.L[0], S.L[1]) * 4.0e-7);
+    simdev_floats(S);
     return S;
 }
 
@@ -340,6 +341,7 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     rc |= dalloc(h, &h->D.nbr, n * k);
     if (mixed) {
         rc |= dalloc(h, &h->D.derf, n);
+        rc |= dalloc(h, &h->D.d2f, n * k);
     } else {
         rc |= dalloc(h, &h->D.der, n);
         rc |= dalloc(h, &h->D.dist, n * k);
@@ -363,8 +365,8 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
         cudaMemcpy(h->d_offs, h->offs.data(), (nsims + 1) * sizeof(int64_t), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(SPH_ERR_CUDA, "device initialisation failed"));
     knn_init_attrs();
-    h->tune.block = k > 48 ? 64 : 128;
-    h->tune.cap = (int)(k + std::max<int64_t>(16, k / 2));
+    h->tune.block = 256;
+    h->tune.cap = (int)(k + 16);
     h->tune.theta = 0.5f;
     h->tune.hgrow = 1.04f;
     h->tune.blocks_per_sm = std::max(1, knn_occupancy_blocks(h->tune.block, h->tune.cap, h->mode));

@@ -58,6 +58,10 @@ struct SimDev {
     double fpref, dfpref;
     float overshoot;       // max distance of a particle outside [lo, lo+L) (periodic axes)
     float tol;             // absolute slack of the FP32 cell tests
+    // FP32 copies used per query (no FP64 instruction in the search's hot path)
+    float fs[2];           // finest cell side
+    float fimg_h[2], fimg_l[2]; // image shifts as float pairs (hi, lo)
+    float flmax;           // max(L)
     unsigned long long bbox[4]; // open axes: ordered-key min x, max x, min y, max y
 };
 
@@ -75,7 +79,9 @@ struct Derived {
     double4 *der;   // FP64 modes: (c, rho, h, c^2/(gamma rho))
     float4 *derf;   // mixed:      (c, rho, h, c^2/(gamma rho))
     int32_t *nbr;   // n*k neighbour codes, slot 0 = nearest
-    double2 *dist;  // FP64 modes: n*k (NNDists, 1/NNDists)
+    double2 *dist;  // FP64 modes: n*k squared distance from the search, then
+                    // (NNDists, NNDists/h) [bit-exact form] or (NNDists, 1/NNDists) [fast form]
+    float *d2f;     // mixed: n*k FP32 squared distances
 };
 
 struct Tables {
@@ -130,6 +136,16 @@ __device__ __forceinline__ int cell_coord(const SimDev &S, int ax, double v) {
     if (!(t >= 0.0)) return 0;
     if (t >= (double)G) return G - 1;
     return (int)t;
+}
+
+// FP32 fields of a SimDev from its FP64 grid fields
+__host__ __device__ inline void simdev_floats(SimDev &S) {
+    for (int a = 0; a < 2; a++) {
+        S.fs[a] = (float)S.s[a];
+        S.fimg_h[a] = (float)S.dimg[a];
+        S.fimg_l[a] = (float)(S.dimg[a] - (double)S.fimg_h[a]);
+    }
+    S.flmax = (float)(S.L[0] > S.L[1] ? S.L[0] : S.L[1]);
 }
 
 // order-preserving 64-bit key of a double (for atomic min/max)

@@ -67,6 +67,7 @@ __global__ void k_grid(Ctx c) {
     }
     double Lm = fmax(S.L[0], S.L[1]);
     S.tol = (float)(Lm * 4.0e-7);
+    simdev_floats(S);
 }
 
 void launch_grid(const Ctx &c, const Launch &L) {

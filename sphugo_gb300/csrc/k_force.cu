@@ -61,8 +61,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                 const uint32_t code = (uint32_t)nb[e];
                 const uint32_t j = code >> kCodeShift;
                 const double d = dist[e].x;
-                const double qq = __ddiv_rn(d, hi);
-                if (qq > 1.0 || qq < 0.0) fl |= FLAG_Q_RANGE;
+                const double qq = dist[e].y;  // NNDists[i]/maxR, the density pass's identical quotient
                 const double drk = kdf_exact(S.kernel, qq);
                 const double4 dj = D.der[j];
                 const double2 vpj = B.vp[j];

@@ -1,24 +1,31 @@
-// k_knn.cu -- exact periodic k-nearest-neighbour search fused with the
-// density, sound speed and pressure term.
+// k_knn.cu -- exact periodic k-nearest-neighbour search (one warp per query
+// particle) and the density / sound-speed pass that consumes its lists.
 //
 // Replaces sim/nearest-neighbour.go:28-165 (nine tree traversals per particle
 // with a sorted insertion queue) and the density / sound-speed loops of
-// sim/sph.go:411-429. One thread per query particle:
+// sim/sph.go:411-429.
+//
+// k_knn, one warp per query:
 //   1. radius guess R (previous smoothing length, or a density estimate from
 //      the cell table at step 0);
-//   2. pick the binning level whose cells are >= theta*R and visit the cells
-//      that intersect the disc of radius R around every periodic image the
-//      reference considers (offsets in {-dX,0,dX} x {-dY,0,dY});
-//   3. FP32 squared distances from float-pair coordinates (error bounded by
-//      eps below) filter candidates into a per-thread list in shared memory;
-//      R is grown or shrunk until the list holds >= k and <= cap entries and
-//      provably contains every candidate that can rank in the top k;
-//   4. candidates whose FP32 order is not certain (within 2 eps of a
-//      neighbour, or of the k-th) are re-ranked with the reference's FP64
-//      squared distance, ties broken by (particle id, image code);
-//   5. density (sim/sph.go:306-323), c = sqrt(gamma(gamma-1) u_pred)
-//      (sim/sph.go:421-429) and c^2/(gamma rho) in the epilogue.
-// The neighbour SET and its order are identical in every arithmetic mode.
+//   2. the binning level whose cells are >= theta*R is chosen and the cells
+//      of the block covering the disc of radius R around the query's images
+//      (offsets in {-dX,0,dX} x {-dY,0,dY}, as the reference) are spread over
+//      the lanes: one cell per lane, a warp prefix sum of their populations;
+//   3. candidates are processed 32 at a time: FP32 squared distances from the
+//      float-pair coordinates filter them against R^2 and a ballot compacts
+//      the survivors into a per-warp list in shared memory; R grows or shrinks
+//      (a warp-uniform decision) until the list holds >= k and <= CAP entries
+//      and provably holds every candidate that can rank in the top k;
+//   4. the list is sorted by a register bitonic network on 32-bit keys
+//      (truncated FP32 squared distance | list slot);
+//   5. every order the FP32 values cannot decide (entries within 2 eps of each
+//      other) is settled with the reference's FP64 squared distance, ties
+//      broken by (particle id, image code); the FP64 forms settle all of them.
+// k_density, one thread per particle: smoothing length h = sqrt of the k-th
+// FP64 squared distance, density (sim/sph.go:306-323),
+// c = sqrt(gamma (gamma-1) u_pred) and c^2/(gamma rho).
+// The neighbour set and its order are identical in every arithmetic form.
 #include "physics.cuh"
 
 #include <algorithm>
@@ -30,79 +37,145 @@ struct KnnArgs {
     PArrays B;
     Derived D;
     const int32_t *start;
-    int cap;
     float theta, hgrow;
 };
 
-// |d2_f32 - d2_ref| <= eps_rel * d2 + eps_abs(R): the float-pair difference
+// |d2_f32 - d2_ref| <= kEpsRel * d2 + eps_abs(R): the float-pair difference
 // carries ~2^-23 relative error, the two float products ~2^-24 each, and the
 // reference's own rounding of (p + offset) adds ~2^-53 L absolute per axis.
 constexpr float kEpsRel = 9.5367431640625e-7f;  // 2^-20 (about 8x the bound)
 
 __device__ __forceinline__ float eps_of(float d2, float abs_term) { return kEpsRel * d2 + abs_term; }
 
-template <int MODE>
-__global__ void __launch_bounds__(128) k_knn(KnnArgs a) {
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <int NR>
+struct ListShape {
+    static constexpr int CAP = 32 * NR;
+    static constexpr int SB = NR == 1 ? 5 : NR == 2 ? 6 : NR == 4 ? 7 : 8;  // slot bits
+    static constexpr uint32_t SMASK = (1u << SB) - 1u;
+};
+
+// Ascending bitonic sort of 32*NR keys, element e = r*32 + lane in v[r].
+template <int NR>
+__device__ __forceinline__ void bitonic_sort(uint32_t (&v)[NR], int lane) {
+    constexpr int N = 32 * NR;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+                const int rs = stride >> 5;
+#pragma unroll
+                for (int r = 0; r < NR; r++) {
+                    const int p = r ^ rs;
+                    if (p > r) {
+                        const bool asc = (((r << 5) | lane) & size) == 0;
+                        const uint32_t a = v[r], b = v[p];
+                        const uint32_t lo = min(a, b), hi = max(a, b);
+                        v[r] = asc ? lo : hi;
+                        v[p] = asc ? hi : lo;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < NR; r++) {
+                    const bool asc = (((r << 5) | lane) & size) == 0;
+                    const bool lower = (lane & stride) == 0;
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, v[r], stride);
+                    v[r] = (asc == lower) ? min(v[r], o) : max(v[r], o);
+                }
+            }
+        }
+    }
+}
+
+// strict order on (exact d2, particle id, image code)
+__device__ __forceinline__ bool exact_greater(const PArrays &B, unsigned long long ka, uint32_t ca,
+                                              unsigned long long kb, uint32_t cb) {
+    if (ka != kb) return ka > kb;
+    const int32_t ia = B.id[ca >> kCodeShift], ib = B.id[cb >> kCodeShift];
+    if (ia != ib) return ia > ib;
+    return (ca & 15u) > (cb & 15u);
+}
+
+template <int MODE, int NR>
+__global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
+    using LS = ListShape<NR>;
+    constexpr int CAP = LS::CAP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int bs = blockDim.x, t = threadIdx.x;
-    const int k = a.c.k, cap = a.cap;
-    unsigned long long *keys = (unsigned long long *)smem_raw;
-    uint32_t *codes = (uint32_t *)(smem_raw + (size_t)cap * bs * 8);
-#define KEY(e) keys[(size_t)(e) * bs + t]
-#define CODE(e) codes[(size_t)(e) * bs + t]
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    // per-warp scratch: exact keys, full FP32 keys, codes, sorted order
+    unsigned char *base = smem_raw + (size_t)w * CAP * 20;
+    unsigned long long *sexact = (unsigned long long *)base;
+    uint32_t *skey = (uint32_t *)(base + CAP * 8);
+    uint32_t *scode = skey + CAP;
+    uint32_t *sord = scode + CAP;
+    const int k = a.c.k;
     const PArrays &B = a.B;
     unsigned fl = 0;
 
-    for (int64_t q = blockIdx.x * (int64_t)bs + t; q < a.c.n; q += (int64_t)gridDim.x * bs) {
+    for (int64_t q = (int64_t)blockIdx.x * wpb + w; q < a.c.n; q += (int64_t)gridDim.x * wpb) {
+        // Only FP32 / integer work below (FP64 would run 32-wide for one query).
         const int s = find_sim(a.c.offs, a.c.nsims, q);
         const SimDev &S = a.c.sims[s];
-        const double2 P = B.pos[q];
         const float4 pr = B.rec[q];
         const float pxr = pr.x + pr.z, pyr = pr.y + pr.w;
-        const int level = S.level, G = 1 << level;
-        const float sx0 = (float)S.s[0], sy0 = (float)S.s[1];
+        const int level = S.level;
+        const float sx0 = S.fs[0], sy0 = S.fs[1], smin = fminf(sx0, sy0);
         const float tol = S.tol + S.overshoot;
         const int per0 = S.periodic[0], per1 = S.periodic[1];
-        const float dXh = __double2float_rn(S.dimg[0]);
-        const float dXl = __double2float_rn(S.dimg[0] - (double)dXh);
-        const float dYh = __double2float_rn(S.dimg[1]);
-        const float dYl = __double2float_rn(S.dimg[1] - (double)dYh);
+        const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
         const int64_t coff = S.cell_off;
-        const float Lmax = (float)fmax(S.L[0], S.L[1]);
-        const float epsabs = 1.8e-15f * Lmax;  // ~2^-49 L: reference rounding of p+offset, float-pair residue
+        const float Lmax = S.flmax;
+        const float epsabs = 1.8e-15f * Lmax;
+        // per-image constants of the float-pair difference (q - offset) - p
+        const float axm = pr.x - dXh, aym = pr.y - dYh;
+        const float cxp = pr.z + dXl, cxm = pr.z - dXl, cyp = pr.w + dYl, cym = pr.w - dYl;
 
-        // ---- radius guess
+        // ---- radius guess (identical in every lane)
         float R = B.hprev[q] * a.hgrow;
         if (!(R > 0.f)) {
-            int cx = cell_coord(S, 0, P.x), cy = cell_coord(S, 1, P.y);
-            float smin = fminf(sx0, sy0);
+            const int G = 1 << level;
+            const int cx = min(max((int)floorf(pxr / sx0), 0), G - 1), cy = min(max((int)floorf(pyr / sy0), 0), G - 1);
             R = 2.f * Lmax;
             for (int sh = 0; sh <= level; sh++) {
-                uint32_t mo = morton2((uint32_t)cx >> sh, (uint32_t)cy >> sh);
-                int n0 = __ldg(a.start + coff + ((int64_t)mo << (2 * sh)));
-                int n1 = __ldg(a.start + coff + ((int64_t)(mo + 1) << (2 * sh)));
-                int cnt = n1 - n0;
+                const uint32_t mo = morton2((uint32_t)cx >> sh, (uint32_t)cy >> sh);
+                const int n0 = __ldg(a.start + coff + ((int64_t)mo << (2 * sh)));
+                const int n1 = __ldg(a.start + coff + ((int64_t)(mo + 1) << (2 * sh)));
+                const int cnt = n1 - n0;
                 if (cnt >= (k + 3) / 4 || sh == level) {
-                    float side = smin * (float)(1 << sh);
+                    const float side = smin * (float)(1 << sh);
                     R = side * sqrtf((float)k / (3.14159265f * fmaxf((float)cnt, 1.f))) * 1.25f;
                     break;
                 }
             }
         }
         const float Rmax = 2.5f * Lmax;
-        float Rlo = 0.f, Rhi = 3.0e38f;
+        float Rlo = 0.f, Rhi = 3.0e38f, tau = 0.f, eps = 0.f;
         int m = 0, ok = 0;
-        float tau = 0.f, eps = 0.f;
+        uint32_t v[NR];
         for (int att = 0; att < 48; att++) {
+            __syncwarp();  // the previous attempt's reads of the list are done
             R = fminf(R, Rmax);
             const float R2 = R * R;
+            // level: smallest sh with smin * 2^sh >= theta * R
             int sh = 0;
             {
-                float smin = fminf(sx0, sy0), want = a.theta * R;
-                while (sh < level && smin * (float)(1 << sh) < want) sh++;
+                const float ratio = a.theta * R / smin;
+                if (ratio > 1.f) {
+                    const int rc = (int)fminf(ceilf(ratio), 1073741824.f);
+                    sh = min(32 - __clz(rc - 1), level);
+                }
             }
-            const int Gl = G >> sh;
-            const float Sx = sx0 * (float)(1 << sh), Sy = sy0 * (float)(1 << sh);
+            const int shift = level - sh;           // Gl = 2^shift cells per axis at this level
+            const int Gl = 1 << shift;
+            const float pw = __int_as_float((127 + sh) << 23);  // 2^sh
+            const float Sx = sx0 * pw, Sy = sy0 * pw;
             const float Re = R + tol;
             int vx0 = (int)floorf((pxr - Re) / Sx), vx1 = (int)floorf((pxr + Re) / Sx);
             int vy0 = (int)floorf((pyr - Re) / Sy), vy1 = (int)floorf((pyr + Re) / Sy);
@@ -110,76 +183,106 @@ __global__ void __launch_bounds__(128) k_knn(KnnArgs a) {
             else { vx0 = max(vx0, 0); vx1 = min(vx1, Gl - 1); }
             if (per1) { vy0 = max(vy0, -Gl); vy1 = min(vy1, 2 * Gl - 1); }
             else { vy0 = max(vy0, 0); vy1 = min(vy1, Gl - 1); }
+            const int nx = max(vx1 - vx0 + 1, 0), ny = max(vy1 - vy0 + 1, 0);
+            const int ncell = nx * ny;
+            const float inv_nx = 1.f / (float)max(nx, 1);
             m = 0;
-            for (int vy = vy0; vy <= vy1; vy++) {
-                const int wy = floordiv(vy, Gl);
-                const int cyl = vy - wy * Gl;
-                const float ylo = (float)vy * Sy;
-                float dyc = fmaxf(fmaxf(ylo - pyr, pyr - (ylo + Sy)) - tol, 0.f);
-                const float dyc2 = dyc * dyc;
-                if (dyc2 > R2) continue;
-                const int ib = -wy;
-                const float By = ib > 0 ? dYh : 0.f;
-                const float Ay = ib < 0 ? pr.y - dYh : pr.y;
-                const float Cy = pr.w + (float)ib * dYl;
-                for (int vx = vx0; vx <= vx1; vx++) {
-                    const int wx = floordiv(vx, Gl);
-                    const int cxl = vx - wx * Gl;
-                    const float xlo = (float)vx * Sx;
-                    float dxc = fmaxf(fmaxf(xlo - pxr, pxr - (xlo + Sx)) - tol, 0.f);
-                    if (dxc * dxc + dyc2 > R2) continue;
-                    const int ia = -wx;
-                    const float Bx = ia > 0 ? dXh : 0.f;
-                    const float Ax = ia < 0 ? pr.x - dXh : pr.x;
-                    const float Cx = pr.z + (float)ia * dXl;
-                    const uint32_t img = (uint32_t)((ia + 1) * 3 + (ib + 1));
-                    const uint32_t mo = morton2((uint32_t)cxl, (uint32_t)cyl);
-                    const int j0 = __ldg(a.start + coff + ((int64_t)mo << (2 * sh)));
-                    const int j1 = __ldg(a.start + coff + ((int64_t)(mo + 1) << (2 * sh)));
-                    for (int j = j0; j < j1; j++) {
+            for (int cb = 0; cb < ncell; cb += 32) {
+                // one cell per lane: its range, image and float-pair constants
+                const int ci = cb + lane;
+                int cbase = 0, cnt = 0;
+                uint32_t img = 4;
+                float Ax = pr.x, Bx = 0.f, Cx = pr.z, Ay = pr.y, By = 0.f, Cy = pr.w;
+                if (ci < ncell) {
+                    const int oy = (int)(((float)ci + 0.5f) * inv_nx);  // exact: ci, nx < 2^20
+                    const int vx = vx0 + (ci - oy * nx), vy = vy0 + oy;
+                    const int wx = vx >> shift, wy = vy >> shift;       // floor division by 2^shift
+                    const float xlo = (float)vx * Sx, ylo = (float)vy * Sy;
+                    const float dxc = fmaxf(fmaxf(xlo - pxr, pxr - (xlo + Sx)) - tol, 0.f);
+                    const float dyc = fmaxf(fmaxf(ylo - pyr, pyr - (ylo + Sy)) - tol, 0.f);
+                    if (dxc * dxc + dyc * dyc <= R2) {
+                        const uint32_t mo = morton2((uint32_t)(vx & (Gl - 1)), (uint32_t)(vy & (Gl - 1)));
+                        const int j0 = __ldg(a.start + coff + ((int64_t)mo << (2 * sh)));
+                        cnt = __ldg(a.start + coff + ((int64_t)(mo + 1) << (2 * sh))) - j0;
+                        img = (uint32_t)((1 - wx) * 3 + (1 - wy));
+                        // image i = -w: hi part of q - i*d exact (Sterbenz) when i = +1,
+                        // of p + i*d when i = -1
+                        if (wx < 0) { Bx = dXh; Cx = cxp; } else if (wx > 0) { Ax = axm; Cx = cxm; }
+                        if (wy < 0) { By = dYh; Cy = cyp; } else if (wy > 0) { Ay = aym; Cy = cym; }
+                        cbase = j0;
+                    }
+                }
+                int inc = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                const int tot = __shfl_sync(0xffffffffu, inc, 31);
+                cbase -= inc - cnt;  // candidate t of this cell is particle cbase + t
+                for (int t0 = 0; t0 < tot; t0 += 32) {
+                    const int t = t0 + lane;
+                    // source lane: the first lane whose inclusive count exceeds t
+                    int src = 0;
+#pragma unroll
+                    for (int b = 16; b > 0; b >>= 1) {
+                        const int iv = __shfl_sync(0xffffffffu, inc, src + b - 1);
+                        if (iv <= t) src += b;
+                    }
+                    const int j = __shfl_sync(0xffffffffu, cbase, src) + t;
+                    const uint32_t simg = __shfl_sync(0xffffffffu, img, src);
+                    const float sAx = __shfl_sync(0xffffffffu, Ax, src), sBx = __shfl_sync(0xffffffffu, Bx, src);
+                    const float sCx = __shfl_sync(0xffffffffu, Cx, src), sAy = __shfl_sync(0xffffffffu, Ay, src);
+                    const float sBy = __shfl_sync(0xffffffffu, By, src), sCy = __shfl_sync(0xffffffffu, Cy, src);
+                    bool pass = false;
+                    float d2 = 0.f;
+                    if (t < tot && j != (int)q) {
                         const float4 r = __ldg(&B.rec[j]);
-                        const float dx = ((r.x - Bx) - Ax) + (r.z - Cx);
-                        const float dy = ((r.y - By) - Ay) + (r.w - Cy);
-                        const float d2 = __fmaf_rn(dx, dx, dy * dy);
-                        if (d2 <= R2 && j != (int)q) {
-                            if (m < cap) {
-                                KEY(m) = __float_as_uint(d2);
-                                CODE(m) = ((uint32_t)j << kCodeShift) | img;
-                            }
-                            m++;
+                        const float dx = ((r.x - sBx) - sAx) + (r.z - sCx);
+                        const float dy = ((r.y - sBy) - sAy) + (r.w - sCy);
+                        d2 = __fmaf_rn(dx, dx, dy * dy);
+                        pass = d2 <= R2;
+                    }
+                    const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+                    if (pass) {
+                        const int pos = m + __popc(bal & lanemask_lt());
+                        if (pos < CAP) {
+                            skey[pos] = __float_as_uint(d2);
+                            scode[pos] = ((uint32_t)j << kCodeShift) | simg;
                         }
                     }
+                    m += __popc(bal);
                 }
             }
             if (m < k) {
                 if (R >= Rmax) { fl |= FLAG_KNN_FEW; break; }
                 Rlo = R;
-                float g = m > 0 ? fmaxf(1.15f, sqrtf((float)k / (float)m) * 1.1f) : 2.f;
+                const float g = m > 0 ? fmaxf(1.15f, sqrtf((float)k / (float)m) * 1.1f) : 2.f;
                 R = Rhi < 3.0e38f ? 0.5f * (Rlo + Rhi) : R * g;
                 continue;
             }
-            if (m > cap) {
+            if (m > CAP) {
                 Rhi = R;
-                float g = sqrtf(0.5f * (float)(k + cap) / (float)m);
+                const float g = sqrtf(0.5f * (float)(k + CAP) / (float)m);
                 R = Rlo > 0.f ? 0.5f * (Rlo + Rhi) : R * g;
                 continue;
             }
-            // sort [0, m) by (approximate d2, code)
-            for (int e = 1; e < m; e++) {
-                unsigned long long kk = KEY(e);
-                uint32_t cc = CODE(e);
-                int f = e - 1;
-                while (f >= 0) {
-                    unsigned long long kf = KEY(f);
-                    if (kf < kk || (kf == kk && CODE(f) < cc)) break;
-                    KEY(f + 1) = kf;
-                    CODE(f + 1) = CODE(f);
-                    f--;
-                }
-                KEY(f + 1) = kk;
-                CODE(f + 1) = cc;
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                const int e = (r << 5) | lane;
+                v[r] = e < m ? ((skey[e] & ~LS::SMASK) | (uint32_t)e) : 0xffffffffu;
             }
-            tau = __uint_as_float((uint32_t)KEY(k - 1));
+            bitonic_sort<NR>(v, lane);
+#pragma unroll
+            for (int r = 0; r < NR; r++) sord[(r << 5) | lane] = v[r] & LS::SMASK;
+            __syncwarp();
+            // tau: the largest FP32 value among the first k in truncated order (>= the k-th smallest)
+            float tmax = 0.f;
+            for (int e = lane; e < k; e += 32) tmax = fmaxf(tmax, __uint_as_float(skey[sord[e]]));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+            tau = tmax;
             eps = eps_of(tau, epsabs * R);
             if (tau + 3.f * eps > R2 * (1.f - 4.8e-7f)) {
                 Rlo = R;
@@ -191,134 +294,162 @@ __global__ void __launch_bounds__(128) k_knn(KnnArgs a) {
         }
         if (!ok) {
             if (!(fl & FLAG_KNN_FEW)) fl |= FLAG_KNN_ATTEMPTS;
-            for (int e = 0; e < k; e++) a.D.nbr[q * k + e] = ((int32_t)q << kCodeShift) | 4;
-            a.D.rho[q] = 0.0; a.D.c[q] = 0.0; a.D.h[q] = 0.0;
-            if (MODE == MODE_MIXED) a.D.derf[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-            else {
-                a.D.der[q] = make_double4(0.0, 0.0, 0.0, 0.0);
-                for (int e = 0; e < k; e++) a.D.dist[q * k + e] = make_double2(0.0, 0.0);
+            for (int e = lane; e < k; e += 32) {
+                a.D.nbr[q * k + e] = ((int32_t)q << kCodeShift) | 4;
+                if (MODE == MODE_MIXED) a.D.d2f[q * k + e] = 0.f;
             }
             continue;
         }
 
-        // ---- exact re-ranking
-        int send = k;
-        {
-            const float lim = tau + 2.f * eps;
-            while (send < m && __uint_as_float((uint32_t)KEY(send)) <= lim) send++;
-        }
-        auto exact_d2 = [&](uint32_t code) -> double {
-            uint32_t j = code >> kCodeShift;
-            double ox, oy;
-            img_shift(S, code & 15u, ox, oy);
-            double2 Q = B.pos[j];
-            return dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
-        };
-        // strict order on (exact d2, particle id, image code)
-        auto exact_greater = [&](unsigned long long ka, uint32_t ca, unsigned long long kb, uint32_t cb) {
-            if (ka != kb) return ka > kb;
-            int32_t ia = B.id[ca >> kCodeShift], ib = B.id[cb >> kCodeShift];
-            if (ia != ib) return ia > ib;
-            return (ca & 15u) > (cb & 15u);
-        };
-        auto exact_sort = [&](int lo, int hi) {  // [lo, hi)
-            for (int e = lo + 1; e < hi; e++) {
-                unsigned long long kk = KEY(e);
-                uint32_t cc = CODE(e);
-                int f = e - 1;
-                while (f >= lo && exact_greater(KEY(f), CODE(f), kk, cc)) {
-                    KEY(f + 1) = KEY(f);
-                    CODE(f + 1) = CODE(f);
-                    f--;
-                }
-                KEY(f + 1) = kk;
-                CODE(f + 1) = cc;
-            }
-        };
-        double dk2 = -1.0;
-        if (MODE != MODE_MIXED) {
-            for (int e = 0; e < send; e++) {
-                uint32_t cc = CODE(e);
-                KEY(e) = (unsigned long long)__double_as_longlong(exact_d2(cc));
-                CODE(e) = cc | kCodeFlag;
-            }
-            exact_sort(0, send);
-            dk2 = __longlong_as_double((long long)KEY(k - 1));
-        } else {
-            int rs = 0;
-            for (int e = 0; e < send; e++) {
-                bool brk = (e + 1 == send);
-                if (!brk) {
-                    float a0 = __uint_as_float((uint32_t)KEY(e)), a1 = __uint_as_float((uint32_t)KEY(e + 1));
-                    brk = (a1 - a0) > 2.f * eps_of(a1, epsabs * R);
-                }
-                if (brk) {
-                    if (e > rs) {
-                        for (int f = rs; f <= e; f++) {
-                            uint32_t cc = CODE(f);
-                            KEY(f) = (unsigned long long)__double_as_longlong(exact_d2(cc));
-                            CODE(f) = cc | kCodeFlag;
-                        }
-                        exact_sort(rs, e + 1);
-                        if (rs <= k - 1 && k - 1 <= e) dk2 = __longlong_as_double((long long)KEY(k - 1));
-                    }
-                    rs = e + 1;
-                }
-            }
-            if (dk2 < 0.0) dk2 = exact_d2(CODE(k - 1));
-        }
-        if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
+        // ---- S = every entry whose FP32 value is within 2 eps of tau (a prefix)
+        const float lim = tau + 2.f * eps;
+        int last = -1;
+        for (int e = lane; e < m; e += 32)
+            if (__uint_as_float(skey[sord[e]]) <= lim) last = e;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+        const int send = last + 1;  // >= k
 
-        // ---- density, sound speed, pressure term
+        // ---- orders the FP32 values cannot decide: FP64 keys, exact runs
+        bool unc = false;
+        for (int e = lane; e + 1 < send; e += 32) {
+            const float fa = __uint_as_float(skey[sord[e]]), fb = __uint_as_float(skey[sord[e + 1]]);
+            unc |= (fb - fa) <= 2.f * eps_of(fb, epsabs * R);
+        }
+        if (__any_sync(0xffffffffu, unc)) {
+            const double2 P = B.pos[q];
+            for (int e = lane; e < send; e += 32) {
+                const float fe = __uint_as_float(skey[sord[e]]);
+                bool need = false;
+                if (e + 1 < send) {
+                    const float fn = __uint_as_float(skey[sord[e + 1]]);
+                    need |= (fn - fe) <= 2.f * eps_of(fn, epsabs * R);
+                }
+                if (e > 0) need |= (fe - __uint_as_float(skey[sord[e - 1]])) <= 2.f * eps_of(fe, epsabs * R);
+                if (need) {
+                    const uint32_t code = scode[sord[e]];
+                    double ox, oy;
+                    img_shift(S, code & 15u, ox, oy);
+                    const double2 Q = B.pos[code >> kCodeShift];
+                    sexact[e] = (unsigned long long)__double_as_longlong(dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y));
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                int rs = 0;
+                for (int e = 0; e < send; e++) {
+                    bool brk = (e + 1 == send);
+                    if (!brk) {
+                        const float fa = __uint_as_float(skey[sord[e]]), fb = __uint_as_float(skey[sord[e + 1]]);
+                        brk = (fb - fa) > 2.f * eps_of(fb, epsabs * R);
+                    }
+                    if (brk) {
+                        // insertion sort of the run [rs, e] by (exact d2, id, image)
+                        for (int x = rs + 1; x <= e; x++) {
+                            const unsigned long long kk = sexact[x];
+                            const uint32_t so = sord[x];
+                            int f = x - 1;
+                            while (f >= rs && exact_greater(B, sexact[f], scode[sord[f]], kk, scode[so])) {
+                                sexact[f + 1] = sexact[f];
+                                sord[f + 1] = sord[f];
+                                f--;
+                            }
+                            sexact[f + 1] = kk;
+                            sord[f + 1] = so;
+                        }
+                        rs = e + 1;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        // ---- write the sorted list (slot 0 = nearest)
+        for (int e = lane; e < k; e += 32) {
+            a.D.nbr[q * k + e] = (int32_t)scode[sord[e]];
+            if (MODE == MODE_MIXED) a.D.d2f[q * k + e] = __uint_as_float(skey[sord[e]]);
+        }
+        __syncwarp();
+    }
+    if (fl && lane == 0) atomicOr(a.c.flags, fl);
+}
+
+// ---------------------------------------------------------------- density
+// the reference's squared distance to the neighbour image a list code names
+__device__ __forceinline__ double nbr_d2(const SimDev &S, const PArrays &B, double2 P, uint32_t code) {
+    double ox, oy;
+    img_shift(S, code & 15u, ox, oy);
+    const double2 Q = B.pos[code >> kCodeShift];
+    return dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_density(KnnArgs a) {
+    const int k = a.c.k;
+    const PArrays &B = a.B;
+    unsigned fl = 0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < a.c.n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int s = find_sim(a.c.offs, a.c.nsims, q);
+        const SimDev &S = a.c.sims[s];
         const double gamma = S.gamma;
         const double up = B.up[q];
         double h, rho, cs, cterm;
         if (MODE == MODE_EXACT64) {
+            // sim/nearest-neighbour.go:64-66 square roots, sim/sph.go:306-323 sum farthest first
+            double2 *dist = a.D.dist + q * k;
+            const double2 P = B.pos[q];
+            const int32_t *nb = a.D.nbr + q * k;
+            const double dk2 = nbr_d2(S, B, P, (uint32_t)nb[k - 1]);
+            if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
             double acc = 0.0;
-            for (int e = k - 1; e >= 0; e--) {  // farthest first, as sim/sph.go:313
-                double d = __dsqrt_rn(__longlong_as_double((long long)KEY(e)));
-                double x = __ddiv_rn(d, h);
+            for (int e = k - 1; e >= 0; e--) {
+                const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, (uint32_t)nb[e]));
+                const double x = __ddiv_rn(d, h);
                 if (x > 1.0 || x < 0.0) fl |= FLAG_Q_RANGE;
                 acc = __dadd_rn(acc, kf_exact(S.kernel, x));
-                a.D.dist[q * k + e] = make_double2(d, 0.0);
+                dist[e] = make_double2(d, x);  // NNDists and q = NNDists/h for the force
             }
             rho = __ddiv_rn(__dmul_rn(__dmul_rn(S.fpref, S.mass), acc), __dmul_rn(h, h));
             cs = __dsqrt_rn(__dmul_rn(__dmul_rn(gamma, __dsub_rn(gamma, 1.0)), up));
             cterm = __ddiv_rn(__dmul_rn(cs, cs), __dmul_rn(gamma, rho));
         } else if (MODE == MODE_FAST64) {
+            double2 *dist = a.D.dist + q * k;
+            const double2 P = B.pos[q];
+            const int32_t *nb = a.D.nbr + q * k;
+            const double dk2 = nbr_d2(S, B, P, (uint32_t)nb[k - 1]);
+            if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
             const double inv_h = 1.0 / h;
             double acc = 0.0;
             for (int e = k - 1; e >= 0; e--) {
-                double d2 = __longlong_as_double((long long)KEY(e));
-                double y = rsqrt(d2);
-                double d = d2 * y;
-                double x = fmin(d * inv_h, 1.0);
+                const double d2 = e == k - 1 ? dk2 : nbr_d2(S, B, P, (uint32_t)nb[e]);
+                const double y = rsqrt(d2);
+                const double d = d2 * y;
+                const double x = fmin(d * inv_h, 1.0);
                 if (!(x >= 0.0)) fl |= FLAG_Q_RANGE;
                 acc += kf_fast(S.kernel, x);
-                a.D.dist[q * k + e] = make_double2(d, y);
+                dist[e] = make_double2(d, y);
             }
             rho = S.fpref * S.mass * acc * (inv_h * inv_h);
             cs = sqrt(gamma * (gamma - 1.0) * up);
             cterm = cs * cs / (gamma * rho);
         } else {
+            // FP64 only where it decides: the k-th neighbour's squared distance and h
+            const double dk2 = nbr_d2(S, B, B.pos[q], (uint32_t)a.D.nbr[q * k + k - 1]);
+            if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
-            const float hf = __double2float_rn(h);
-            const float inv_hf = 1.f / hf;
+            const float inv_hf = 1.f / __double2float_rn(h);
+            const float *d2f = a.D.d2f + q * k;
             KahanF acc;
             for (int e = k - 1; e >= 0; e--) {
-                unsigned long long kk = KEY(e);
-                float d2 = (CODE(e) & kCodeFlag) ? __double2float_rn(__longlong_as_double((long long)kk))
-                                                 : __uint_as_float((uint32_t)kk);
-                float x = fminf(sqrtf(d2) * inv_hf, 1.f);
+                const float x = fminf(sqrtf(d2f[e]) * inv_hf, 1.f);
                 acc.add(kf_f32(S.kernel, x));
             }
             rho = (S.fpref * S.mass / (h * h)) * acc.value();
             cs = sqrt(gamma * (gamma - 1.0) * up);
             cterm = cs * cs / (gamma * rho);
         }
-        for (int e = 0; e < k; e++) a.D.nbr[q * k + e] = (int32_t)(CODE(e) & ~kCodeFlag);
         a.D.rho[q] = rho;
         a.D.c[q] = cs;
         a.D.h[q] = h;
@@ -328,39 +459,68 @@ __global__ void __launch_bounds__(128) k_knn(KnnArgs a) {
             a.D.der[q] = make_double4(cs, rho, h, cterm);
     }
     if (fl) atomicOr(a.c.flags, fl);
-#undef KEY
-#undef CODE
 }
 
-static size_t knn_smem(int block, int cap) { return (size_t)cap * block * 12; }
+// ---------------------------------------------------------------- launch
+constexpr int kKnnBlock = 256;
+
+static int list_regs(int k) {
+    const int need = (3 * k) / 2 + 8;
+    return need <= 32 ? 1 : need <= 64 ? 2 : need <= 128 ? 4 : 8;
+}
+static size_t knn_smem(int nr) { return (size_t)(kKnnBlock / 32) * 32 * nr * 20; }
+
+template <int MODE, int NR>
+static void knn_attr() {
+    cudaFuncSetAttribute(k_knn<MODE, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)knn_smem(NR));
+}
+template <int MODE>
+static void knn_attrs_mode() {
+    knn_attr<MODE, 1>();
+    knn_attr<MODE, 2>();
+    knn_attr<MODE, 4>();
+    knn_attr<MODE, 8>();
+}
 
 // Sets the dynamic shared-memory limit of every instantiation; must run
 // before any stream capture.
 void knn_init_attrs() {
-    cudaFuncSetAttribute(k_knn<MODE_EXACT64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_knn<MODE_FAST64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_knn<MODE_MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    knn_attrs_mode<MODE_EXACT64>();
+    knn_attrs_mode<MODE_FAST64>();
+    knn_attrs_mode<MODE_MIXED>();
 }
 
-int knn_occupancy_blocks(int block, int cap, int mode) {
+template <int MODE, int NR>
+static int occ(int) {
     int nb = 0;
-    size_t smem = knn_smem(block, cap);
-    if (mode == MODE_EXACT64)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_knn<MODE_EXACT64>, block, smem);
-    else if (mode == MODE_FAST64)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_knn<MODE_FAST64>, block, smem);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_knn<MODE_MIXED>, block, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_knn<MODE, NR>, kKnnBlock, knn_smem(NR));
     return nb;
+}
+
+int knn_occupancy_blocks(int, int cap, int mode) {
+    // cap carries k + slack; the list shape follows k
+    const int nr = list_regs(std::max(1, cap - 16));
+    auto pick = [&](auto f1, auto f2, auto f4, auto f8) { return nr == 1 ? f1(0) : nr == 2 ? f2(0) : nr == 4 ? f4(0) : f8(0); };
+    if (mode == MODE_EXACT64) return pick(occ<MODE_EXACT64, 1>, occ<MODE_EXACT64, 2>, occ<MODE_EXACT64, 4>, occ<MODE_EXACT64, 8>);
+    if (mode == MODE_FAST64) return pick(occ<MODE_FAST64, 1>, occ<MODE_FAST64, 2>, occ<MODE_FAST64, 4>, occ<MODE_FAST64, 8>);
+    return pick(occ<MODE_MIXED, 1>, occ<MODE_MIXED, 2>, occ<MODE_MIXED, 4>, occ<MODE_MIXED, 8>);
 }
 
 template <int MODE>
 static void run_knn(const KnnArgs &args, const Launch &L, const KnnTune &tune) {
-    size_t smem = knn_smem(tune.block, args.cap);
-    int64_t need = (args.c.n + tune.block - 1) / tune.block;
+    const int nr = list_regs(args.c.k);
+    const int wpb = kKnnBlock / 32;
+    const int64_t need = (args.c.n + wpb - 1) / wpb;
     int grid = (int)std::min<int64_t>(need, (int64_t)L.sms * std::max(tune.blocks_per_sm, 1));
     if (grid < 1) grid = 1;
-    k_knn<MODE><<<grid, tune.block, smem, L.stream>>>(args);
+    const size_t smem = knn_smem(nr);
+    if (nr == 1) k_knn<MODE, 1><<<grid, kKnnBlock, smem, L.stream>>>(args);
+    else if (nr == 2) k_knn<MODE, 2><<<grid, kKnnBlock, smem, L.stream>>>(args);
+    else if (nr == 4) k_knn<MODE, 4><<<grid, kKnnBlock, smem, L.stream>>>(args);
+    else k_knn<MODE, 8><<<grid, kKnnBlock, smem, L.stream>>>(args);
+    const int64_t dneed = (args.c.n + 255) / 256;
+    const int dgrid = (int)std::max<int64_t>(1, std::min<int64_t>(dneed, (int64_t)L.sms * 8));
+    k_density<MODE><<<dgrid, 256, 0, L.stream>>>(args);
 }
 
 void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D,
@@ -370,7 +530,6 @@ void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &
     a.B = B;
     a.D = D;
     a.start = T.start;
-    a.cap = tune.cap;
     a.theta = tune.theta;
     a.hgrow = tune.hgrow;
     if (mode == MODE_EXACT64) run_knn<MODE_EXACT64>(a, L, tune);

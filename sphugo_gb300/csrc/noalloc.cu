@@ -187,6 +187,7 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     S.fpref = p->kernel == SPH_KERNEL_WENDLAND ? kWendFPref : kMonahanPref;
     S.dfpref = p->kernel == SPH_KERNEL_WENDLAND ? kWendDFPref : kMonahanPref;
     S.tol = (float)(std::max(S.L[0], S.L[1]) * 4.0e-7);
+    simdev_floats(S);
     T.ncells = (int64_t)1 << (2 * S.level);
     const bool any_open = !S.periodic[0] || !S.periodic[1];
 
