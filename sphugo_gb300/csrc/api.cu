@@ -213,6 +213,7 @@ void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) 
     launch_bin(c, L, h->A, h->T, pred);
     mark(1);
     launch_scan(c, L, h->T);
+    launch_stable(c, L, h->T);
     mark(2);
     launch_permute(c, L, h->A, h->B, h->T, pred, h->mode == MODE_MIXED);
     mark(3);
@@ -349,6 +350,7 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     h->T.ncells = cells;
     rc |= dalloc(h, &h->T.key, n);
     rc |= dalloc(h, &h->T.rank, n);
+    rc |= dalloc(h, &h->T.tmp, n);
     rc |= dalloc(h, &h->T.count, cells);
     rc |= dalloc(h, &h->T.start, cells + 1);
     rc |= dalloc(h, &h->T.partial, cells / 4096 + 2);

@@ -85,7 +85,8 @@ struct Derived {
 };
 
 struct Tables {
-    int32_t *key, *rank;   // per particle
+    int32_t *key, *rank;   // per particle (rank becomes the destination slot)
+    int32_t *tmp;          // per particle: source indices grouped by cell
     int32_t *count;        // per cell (zero between binnings)
     int32_t *start;        // per cell + 1
     int32_t *partial;      // scan block sums
@@ -199,6 +200,7 @@ void launch_bbox(const Ctx &c, const Launch &L, const PArrays &A, int pred);
 void launch_grid(const Ctx &c, const Launch &L);
 void launch_bin(const Ctx &c, const Launch &L, const PArrays &A, const Tables &T, int pred);
 void launch_scan(const Ctx &c, const Launch &L, const Tables &T);
+void launch_stable(const Ctx &c, const Launch &L, const Tables &T);
 void launch_permute(const Ctx &c, const Launch &L, const PArrays &A, const PArrays &B,
                     const Tables &T, int pred, bool mixed);
 

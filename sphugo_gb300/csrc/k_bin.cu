@@ -198,6 +198,45 @@ void launch_scan(const Ctx &, const Launch &L, const Tables &T) {
     k_scan_final<<<ntiles, kScanThreads, 0, L.stream>>>(T);
 }
 
+// ---------------------------------------------------------- stable order
+// The histogram's atomic ranks order a cell's particles arbitrarily. To make
+// every later order (and so every floating-point sum) reproducible, each
+// cell's members are re-ranked by their index in the previous order: group
+// the source indices by cell, sort each cell's group (one thread per cell;
+// cells hold a few particles at the automatic level), and store each
+// particle's destination slot in T.rank.
+__global__ void k_group(Ctx c, Tables T) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        T.tmp[T.start[T.key[i]] + T.rank[i]] = (int32_t)i;
+}
+
+__global__ void k_cell_order(Tables T) {
+    for (int64_t cidx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; cidx < T.ncells;
+         cidx += (int64_t)gridDim.x * blockDim.x) {
+        const int a = T.start[cidx], b = T.start[cidx + 1];
+        if (b - a > 1) {
+            for (int x = a + 1; x < b; x++) {
+                const int32_t v = T.tmp[x];
+                int f = x - 1;
+                while (f >= a && T.tmp[f] > v) {
+                    T.tmp[f + 1] = T.tmp[f];
+                    f--;
+                }
+                T.tmp[f + 1] = v;
+            }
+        }
+        for (int x = a; x < b; x++) T.rank[T.tmp[x]] = x;
+    }
+}
+
+void launch_stable(const Ctx &c, const Launch &L, const Tables &T) {
+    k_group<<<L.sms * 8, 256, 0, L.stream>>>(c, T);
+    const int64_t need = (T.ncells + 255) / 256;
+    const int grid = (int)(need < (int64_t)L.sms * 16 ? need : (int64_t)L.sms * 16);
+    k_cell_order<<<grid > 0 ? grid : 1, 256, 0, L.stream>>>(T);
+}
+
 // --------------------------------------------------------------- permute
 // Writes the predicted state into cell order (B), plus the float-pair
 // position record relative to the grid origin used by the FP32 distance
@@ -207,7 +246,7 @@ __global__ void k_permute(Ctx c, PArrays A, PArrays B, Tables T, int pred, int m
          i += (int64_t)gridDim.x * blockDim.x) {
         int s = find_sim(c.offs, c.nsims, i);
         const SimDev &S = c.sims[s];
-        int64_t d = (int64_t)T.start[T.key[i]] + T.rank[i];
+        const int64_t d = T.rank[i];  // destination slot (stable within the cell)
         double2 pos = A.pos[i], vel = A.vel[i];
         double u = A.u[i];
         double2 p, vp;

@@ -268,6 +268,80 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
                 continue;
             }
             __syncwarp();
+            if (MODE == MODE_MIXED) {
+                // The mixed form needs the set, not the order: drop the m-k
+                // largest (unique keys: truncated FP32 value | slot) by warp
+                // max-reductions, then verify with the full FP32 values that
+                // every kept entry lies more than 2 eps below every dropped one
+                // and that the farthest kept entry is unique by 2 eps.
+#pragma unroll
+                for (int r = 0; r < NR; r++) {
+                    const int e = (r << 5) | lane;
+                    // bit 31 tags a live entry (FP32 squared distances are >= 0)
+                    v[r] = e < m ? (0x80000000u | (skey[e] & ~LS::SMASK) | (uint32_t)e) : 0u;
+                }
+                uint32_t dropped_min = 0xffffffffu;  // smallest full FP32 bits among dropped entries
+                for (int it = 0; it < m - k; it++) {
+                    uint32_t lm = 0;
+#pragma unroll
+                    for (int r = 0; r < NR; r++) lm = max(lm, v[r]);
+                    const uint32_t gm = __reduce_max_sync(0xffffffffu, lm);
+#pragma unroll
+                    for (int r = 0; r < NR; r++)
+                        if (v[r] == gm) v[r] = 0u;
+                    dropped_min = min(dropped_min, skey[gm & LS::SMASK]);
+                }
+                // largest and second largest full values among the kept entries
+                uint32_t top = 0, second = 0;  // tagged with bit 31 when set
+#pragma unroll
+                for (int r = 0; r < NR; r++) {
+                    if (v[r]) {
+                        const uint32_t f = 0x80000000u | skey[v[r] & LS::SMASK];
+                        if (f > top) { second = top; top = f; } else if (f > second) second = f;
+                    }
+                }
+                const uint32_t gtop = __reduce_max_sync(0xffffffffu, top);
+                // second: the largest of (each lane's top unless it is the global top) and seconds
+                const uint32_t cand2 = top == gtop ? second : top;
+                const uint32_t g2 = __reduce_max_sync(0xffffffffu, cand2);
+                const uint32_t nties = __popc(__ballot_sync(0xffffffffu, top == gtop));
+                tau = __uint_as_float(gtop & 0x7fffffffu);
+                eps = eps_of(tau, epsabs * R);
+                if (tau + 3.f * eps > R2 * (1.f - 4.8e-7f)) {
+                    Rlo = R;
+                    R = sqrtf((tau + 3.f * eps) * 1.00002f) * 1.0001f;
+                    continue;
+                }
+                const float fd = __uint_as_float(dropped_min), f2 = __uint_as_float(g2 & 0x7fffffffu);
+                const bool set_ok = (m == k) || (fd - tau > 2.f * eps_of(fd, epsabs * R));
+                const bool top_ok = nties == 1 && (k == 1 || tau - f2 > 2.f * eps);
+                if (set_ok && top_ok) {
+                    // write the kept entries in slot order, the farthest last
+                    int pos = 0;
+#pragma unroll
+                    for (int r = 0; r < NR; r++) {
+                        const bool live = v[r] != 0u;
+                        const bool is_top = live && (0x80000000u | skey[v[r] & LS::SMASK]) == gtop;
+                        const bool keep = live && !is_top;
+                        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+                        if (keep) {
+                            const int o = pos + __popc(bal & lanemask_lt());
+                            const uint32_t sl = v[r] & LS::SMASK;
+                            a.D.nbr[q * k + o] = (int32_t)scode[sl];
+                            a.D.d2f[q * k + o] = __uint_as_float(skey[sl]);
+                        }
+                        if (is_top) {
+                            const uint32_t sl = v[r] & LS::SMASK;
+                            a.D.nbr[q * k + k - 1] = (int32_t)scode[sl];
+                            a.D.d2f[q * k + k - 1] = __uint_as_float(skey[sl]);
+                        }
+                        pos += __popc(bal);
+                    }
+                    ok = 2;  // written
+                    break;
+                }
+                // otherwise fall through to the sorted path below
+            }
 #pragma unroll
             for (int r = 0; r < NR; r++) {
                 const int e = (r << 5) | lane;
@@ -298,6 +372,10 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
                 a.D.nbr[q * k + e] = ((int32_t)q << kCodeShift) | 4;
                 if (MODE == MODE_MIXED) a.D.d2f[q * k + e] = 0.f;
             }
+            continue;
+        }
+        if (ok == 2) {
+            __syncwarp();
             continue;
         }
 

@@ -90,40 +90,53 @@ void launch_gather_derived(const Ctx &c, const Launch &L, const PArrays &A, cons
 }
 
 // Reference layout: slot 0 = farthest (sim/nearest-neighbour.go:139-153 keeps
-// NNDists descending). dist = sqrt of the reference's squared distance.
-__global__ void k_gather_nbrs(Ctx c, PArrays B, Derived D, int have_dist, int64_t *ids, double *dist,
-                              int32_t *img) {
+// NNDists descending); dist = sqrt of the reference's squared distance. Lists
+// are re-sorted here by (squared distance, particle id, image code): the
+// mixed form stores its neighbour set unordered.
+constexpr int kMaxK = 128;
+
+__global__ void k_gather_nbrs(Ctx c, PArrays B, Derived D, int64_t *ids, double *dist, int32_t *img) {
     const int k = c.k;
     GRID_STRIDE(i, c.n) {
         const int s = find_sim(c.offs, c.nsims, i);
         const SimDev &S = c.sims[s];
         const int64_t idq = B.id[i];
         const double2 P = B.pos[i];
+        double d2[kMaxK];
+        uint32_t cd[kMaxK];
         for (int e = 0; e < k; e++) {
-            uint32_t code = (uint32_t)D.nbr[i * k + e];
-            uint32_t j = code >> kCodeShift;
-            int64_t o = idq * k + (k - 1 - e);
-            if (ids) ids[o] = B.id[j];
-            if (img) img[o] = (int32_t)(code & 15u);
-            if (dist) {
-                if (have_dist) {
-                    dist[o] = D.dist[i * k + e].x;
-                } else {
-                    double ox, oy;
-                    img_shift(S, code & 15u, ox, oy);
-                    double2 Q = B.pos[j];
-                    dist[o] = __dsqrt_rn(dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y));
+            const uint32_t code = (uint32_t)D.nbr[i * k + e];
+            double ox, oy;
+            img_shift(S, code & 15u, ox, oy);
+            const double2 Q = B.pos[code >> kCodeShift];
+            const double v = dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
+            int f = e - 1;
+            while (f >= 0) {
+                bool gt = d2[f] > v;
+                if (d2[f] == v) {
+                    const int32_t ia = B.id[cd[f] >> kCodeShift], ib = B.id[code >> kCodeShift];
+                    gt = ia != ib ? ia > ib : (cd[f] & 15u) > (code & 15u);
                 }
+                if (!gt) break;
+                d2[f + 1] = d2[f];
+                cd[f + 1] = cd[f];
+                f--;
             }
+            d2[f + 1] = v;
+            cd[f + 1] = code;
+        }
+        for (int e = 0; e < k; e++) {
+            const int64_t o = idq * k + (k - 1 - e);
+            if (ids) ids[o] = B.id[cd[e] >> kCodeShift];
+            if (img) img[o] = (int32_t)(cd[e] & 15u);
+            if (dist) dist[o] = __dsqrt_rn(d2[e]);
         }
     }
 }
 
-// The FP64 form stores the reference's NNDists; the others recompute them
-// from the evaluation's positions (their stored distances are approximations).
 void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &, const PArrays &B,
-                              const Derived &D, int64_t *ids, double *dist, int32_t *img, bool exact_stored) {
-    k_gather_nbrs<<<grid_for(L, c.n, 128), 128, 0, L.stream>>>(c, B, D, exact_stored ? 1 : 0, ids, dist, img);
+                              const Derived &D, int64_t *ids, double *dist, int32_t *img, bool) {
+    k_gather_nbrs<<<grid_for(L, c.n, 128), 128, 0, L.stream>>>(c, B, D, ids, dist, img);
 }
 
 // ---- diagnostics: deterministic sums over the caller's particle order.

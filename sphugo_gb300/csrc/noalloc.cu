@@ -34,7 +34,7 @@ constexpr size_t kPArraysBytes = 4 * align256(16 * kN) + 3 * align256(8 * kN) + 
 constexpr size_t kScratchBytes =
     2 * kPArraysBytes +                                                        // A, B
     3 * align256(8 * kN) + align256(32 * kN) + align256(4 * kNK) + align256(16 * kNK) +  // D
-    2 * align256(4 * kN) + align256(4 * kNoAllocCells) + align256(4 * (kNoAllocCells + 1)) +
+    3 * align256(4 * kN) + align256(4 * kNoAllocCells) + align256(4 * (kNoAllocCells + 1)) +
     align256(4 * (kNoAllocCells / 4096 + 2)) +                               // T
     align256(sizeof(SimDev)) + align256(2 * sizeof(int64_t)) + align256(sizeof(unsigned));
 
@@ -153,6 +153,7 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     Tables T{};
     T.key = cv.take<int32_t>(kN);
     T.rank = cv.take<int32_t>(kN);
+    T.tmp = cv.take<int32_t>(kN);
     T.count = cv.take<int32_t>(kNoAllocCells);
     T.start = cv.take<int32_t>(kNoAllocCells + 1);
     T.partial = cv.take<int32_t>(kNoAllocCells / 4096 + 2);
@@ -214,6 +215,7 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     }
     launch_bin(c, L, A, T, PRED_INIT);
     launch_scan(c, L, T);
+    launch_stable(c, L, T);
     launch_permute(c, L, A, B, T, PRED_INIT, false);
     launch_knn(c, L, B, D, T, MODE_EXACT64, tune);
     if (nbr_ids || nbr_dist) launch_gather_neighbours(c, L, B, B, D, nbr_ids, nbr_dist, nullptr, true);
