@@ -151,12 +151,15 @@ def measured_peaks():
         return {}
 
 
-def make_sim(n, precision, seed):
+def make_sim(n, precision, seed, tune=True):
+    """The workload's simulation, autotuned (the tuner caches its choice)."""
     from sphugo_gb300 import ics
     from sphugo_gb300 import sim as S
     conf = ics.periodic_config(n, K_NEIGH, DT, precision)
     arrs = ics.uniform_blast(n, seed)
-    return S.Simulation(conf, *arrs)
+    sim = S.Simulation(conf, *arrs)
+    sim.tune_report = sim.Autotune() if tune else None
+    return sim
 
 
 def timed(sim, steps):
@@ -205,11 +208,12 @@ def workload_case(kind, n, k, dt, seed, form, steps, grid_level=0):
     arrs = {"clustered": ics.clustered, "stress": ics.stress}[kind](n, seed)
     conf = ics.periodic_config(n, k, dt, form, grid_level=grid_level)
     sim = S.Simulation(conf, *arrs)
+    tune = sim.Autotune()
     sim.Step(2)
     ms = timed(sim, steps)
     st = profile(sim, 2)
     sim.close()
-    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st}
+    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st, "tune": tune}
 
 
 def e2e_run(sim, steps):
@@ -308,6 +312,7 @@ def run_ours(args, dist):
 
     form = {"exact": "Exact", "fast": "Fast", "mixed": "Mixed"}[args.form]
     sim = make_sim(n, form, SEED + 1000 * dist.rank)
+    tune_report = sim.tune_report
     sim.Step(W)
     kernels = int(lib.sph_kernels_per_step(sim._h))
     clk = ClockSampler(dist.local)
@@ -357,7 +362,8 @@ def run_ours(args, dist):
             s2.Step(W)
             t = timed(s2, K)
             extras[{"Fast": "fp64_fast", "Mixed": "mixed"}[form]] = {
-                "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3)}
+                "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3),
+                "tune": s2.tune_report}
             s2.close()
         extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
         ens = {}
@@ -390,6 +396,7 @@ def run_ours(args, dist):
             "clocks": clocks, "e2e": e2e, "gpu_launches": kernels * K, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu, "tolerances": TOLERANCES,
             "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value}, "forms": extras,
+            "tune": tune_report,
         }
         print(json.dumps(line), flush=True)
     return 0

@@ -120,6 +120,15 @@ int sph_synchronize(sph_handle *h);
 int32_t sph_current_step(const sph_handle *h);
 int64_t sph_num_particles(const sph_handle *h);
 
+/* ---- checkpoint / resume (no reference counterpart) ----
+ * sph_save writes a versioned binary file: a header (sizes, step counter,
+ * binning level, a hash of the parameters and simulation sizes) and the
+ * integrator state in the device's storage order, so that a run resumed with
+ * sph_load on a handle created with the same parameters continues bit for
+ * bit in every arithmetic form. */
+int sph_save(sph_handle *h, const char *path);
+int sph_load(sph_handle *h, const char *path);
+
 /* ---- measurement (no reference counterpart) ---- */
 #define SPH_NUM_STAGES 5   /* bin (incl. prep/bbox), scan, permute, knn+density, force+integrate */
 /* sph_step with the device time between CUDA events recorded on the
@@ -131,6 +140,18 @@ int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms);
 int sph_step_profiled(sph_handle *h, int32_t nsteps, double stage_ms[SPH_NUM_STAGES]);
 /* Kernel launches of one regular step (graph kernel nodes). */
 int32_t sph_kernels_per_step(sph_handle *h);
+/* Autotuner (no reference counterpart): on a freshly uploaded state (before
+ * the first step) it times forces-only evaluations over a small grid of the
+ * neighbour search's shape (cell side / search radius factor, radius-guess
+ * growth, automatic binning level -1..+1, or -1..+2 for clustered data),
+ * keeps the fastest, restores the
+ * uploaded state and caches the choice per (particle count in half octaves,
+ * k, arithmetic form, single/ensemble, distribution class from the spread of
+ * smoothing lengths) in the text file named by SPHGPU_TUNE_CACHE (default
+ * $HOME/.cache/sphgpu/tune.txt). With use_cache the cached choice is applied
+ * without timing. Results do not depend on the choice; only speed does.
+ * report (may be NULL) receives a one-line JSON summary. */
+int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_len);
 /* Arithmetic throughput probe on the current device: FP64 FMA and FP32 FMA
  * in TFLOP/s (2 flops per FMA), from independent FMA chains. */
 int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops);
@@ -155,6 +176,13 @@ int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops);
 #define SPH_NOALLOC_MAX_K 32
 int sph_density_noalloc(const sph_params *p, const double *x, const double *y, int32_t n, int64_t *nbr_ids,
                         double *nbr_dist, double *rho, double *hsml, void *stream);
+
+/* Self-check (no reference counterpart): runs the library's FMA-based
+ * correctly rounded divisions (a shared reciprocal with one Markstein
+ * correction, and division by 3) against the hardware division on n seeded
+ * operand pairs, half of them built to lie next to rounding midpoints, and
+ * reports the number of results that differ (0 expected). */
+int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches);
 
 /* Page-locks (pins) caller memory so that transfers from / to it run at
  * full link speed; no reference counterpart. */

@@ -41,7 +41,7 @@ EXPORTS = [
     "sph_ic_stress", "sph_ic_ensemble", "sph_config_default", "sph_config_load",
     "sph_config_start_count", "sph_config_spawn", "sph_point_source_spawn",
     "sph_step_timed", "sph_step_profiled", "sph_kernels_per_step", "sph_probe_peaks",
-    "sph_density_noalloc",
+    "sph_density_noalloc", "sph_autotune", "sph_save", "sph_load", "sph_selftest_division",
 ]
 NOALLOC_MAX_N = 8192
 NOALLOC_MAX_K = 32
@@ -142,6 +142,10 @@ def load() -> C.CDLL:
     L.sph_kernels_per_step.argtypes = [vp]
     L.sph_kernels_per_step.restype = C.c_int32
     L.sph_probe_peaks.argtypes = [dp, dp]
+    L.sph_autotune.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
+    L.sph_save.argtypes = [vp, C.c_char_p]
+    L.sph_selftest_division.argtypes = [C.c_int64, C.c_uint64, i64p]
+    L.sph_load.argtypes = [vp, C.c_char_p]
     L.sph_density_noalloc.argtypes = [C.POINTER(SphParams), vp, vp, C.c_int32, vp, vp, vp, vp, vp]
     _lib = L
     return L

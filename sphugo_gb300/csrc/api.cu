@@ -10,8 +10,12 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <filesystem>
+#include <fstream>
 #include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -60,12 +64,17 @@ struct sph_handle {
     std::vector<SimDev> hsims;
     SimDev *d_sims = nullptr;
     int64_t *d_offs = nullptr;
+    int32_t *d_simidx = nullptr;
     unsigned *d_flags = nullptr;
     PArrays A{}, B{};
     Derived D{};
     Tables T{};
     KnnTune tune{};
     bool any_open = false, uploaded = false, evaluated = false;
+    std::vector<int> base_level;  // per simulation; explicit grid_level or automatic
+    std::vector<bool> auto_lvl;   // true when the level is the automatic one (the tuner may shift it)
+    int level_delta = 0;
+    int64_t cells_cap = 0;
     int32_t step = 0;
     cudaGraphExec_t g_step = nullptr, g_init = nullptr, g_forces = nullptr, g_prof = nullptr;
     cudaEvent_t ev[SPH_NUM_STAGES + 1] = {};
@@ -81,6 +90,7 @@ struct sph_handle {
         c.sims = d_sims;
         c.sims_rw = d_sims;
         c.offs = d_offs;
+        c.simidx = nsims > 1 ? d_simidx : nullptr;
         c.nsims = nsims;
         c.n = n;
         c.k = k;
@@ -308,15 +318,21 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     h->params.assign(params, params + nsims);
     h->offs.resize(nsims + 1);
     h->offs[0] = 0;
-    int64_t cells = 0;
+    int64_t cells = 0, cap = 0;
     for (int s = 0; s < nsims; s++) {
         h->offs[s + 1] = h->offs[s] + counts[s];
-        int level = params[s].grid_level > 0 ? params[s].grid_level : auto_level(counts[s]);
+        const bool autol = params[s].grid_level <= 0;
+        int level = autol ? auto_level(counts[s]) : params[s].grid_level;
+        h->base_level.push_back(level);
+        h->auto_lvl.push_back(autol);
         h->hsims.push_back(make_simdev(params[s], h->offs[s], counts[s], cells, level));
         h->any_open = h->any_open || !h->hsims.back().periodic[0] || !h->hsims.back().periodic[1];
         cells += (int64_t)1 << (2 * level);
+        // room for the tuner to refine an automatic level by up to two
+        cap += (int64_t)1 << (2 * (autol ? std::min(level + 2, kMaxLevel) : level));
     }
-    if (cells >= ((int64_t)1 << 31) - 1) {
+    h->cells_cap = cap;
+    if (cap >= ((int64_t)1 << 31) - 1) {
         delete h;
         return fail(SPH_ERR_ARG, "cell tables exceed 2^31 cells; lower grid_level");
     }
@@ -333,6 +349,7 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     const int64_t n = h->n, k = h->k;
     rc |= dalloc(h, &h->d_sims, nsims);
     rc |= dalloc(h, &h->d_offs, nsims + 1);
+    if (nsims > 1) rc |= dalloc(h, &h->d_simidx, total);
     rc |= dalloc(h, &h->d_flags, 1);
     if (rc) return bail(SPH_ERR_NOMEM);
     if (alloc_parrays(h, h->A, mixed) || alloc_parrays(h, h->B, mixed)) return bail(SPH_ERR_NOMEM);
@@ -351,13 +368,13 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     rc |= dalloc(h, &h->T.key, n);
     rc |= dalloc(h, &h->T.rank, n);
     rc |= dalloc(h, &h->T.tmp, n);
-    rc |= dalloc(h, &h->T.count, cells);
-    rc |= dalloc(h, &h->T.start, cells + 1);
-    rc |= dalloc(h, &h->T.partial, cells / 4096 + 2);
+    rc |= dalloc(h, &h->T.count, cap);
+    rc |= dalloc(h, &h->T.start, cap + 1);
+    rc |= dalloc(h, &h->T.partial, cap / 4096 + 2);
     h->io_doubles = (size_t)std::max<int64_t>(8 * n, 3 * n + 512);
     rc |= dalloc(h, &h->d_io, h->io_doubles);
     if (rc) return bail(SPH_ERR_NOMEM);
-    if (cudaMemset(h->T.count, 0, cells * sizeof(int32_t)) != cudaSuccess ||
+    if (cudaMemset(h->T.count, 0, cap * sizeof(int32_t)) != cudaSuccess ||
         cudaMemset(h->D.nbr, 0, n * k * sizeof(int32_t)) != cudaSuccess ||
         cudaMemset(h->B.id, 0, n * sizeof(int32_t)) != cudaSuccess ||
         cudaMemset(h->A.id, 0, n * sizeof(int32_t)) != cudaSuccess ||
@@ -366,6 +383,13 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
         cudaMemcpy(h->d_sims, h->hsims.data(), nsims * sizeof(SimDev), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(h->d_offs, h->offs.data(), (nsims + 1) * sizeof(int64_t), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(SPH_ERR_CUDA, "device initialisation failed"));
+    if (nsims > 1) {
+        std::vector<int32_t> idx((size_t)total);
+        for (int s = 0; s < nsims; s++)
+            for (int64_t i = h->offs[s]; i < h->offs[s + 1]; i++) idx[(size_t)i] = s;
+        if (cudaMemcpy(h->d_simidx, idx.data(), total * sizeof(int32_t), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(SPH_ERR_CUDA, "device initialisation failed"));
+    }
     knn_init_attrs();
     h->tune.block = 256;
     h->tune.cap = (int)(k + 16);
@@ -387,6 +411,98 @@ int copy_out(sph_handle *h, double *dst, const double *src) {
     if (!dst) return SPH_OK;
     CUDA_TRY(cudaMemcpyAsync(dst, src, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return SPH_OK;
+}
+
+// ------------------------------------------------------------------ tuning
+// Rebuilds the cell-table layout for binning levels base + delta (automatic
+// levels only); graphs captured with the old layout are dropped.
+int apply_levels(sph_handle *h, int delta) {
+    int64_t cells = 0;
+    for (int s = 0; s < h->nsims; s++) {
+        int level = h->base_level[s];
+        if (h->auto_lvl[s]) level = std::min(std::max(level + delta, 1), kMaxLevel);
+        SimDev S = make_simdev(h->params[s], h->offs[s], h->offs[s + 1] - h->offs[s], cells, level);
+        h->hsims[s] = S;
+        cells += (int64_t)1 << (2 * level);
+    }
+    if (cells > h->cells_cap) return fail(SPH_ERR_ARG, "binning level beyond the allocated cell table");
+    CUDA_TRY(cudaMemcpyAsync(h->d_sims, h->hsims.data(), h->nsims * sizeof(SimDev), cudaMemcpyHostToDevice,
+                             h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->T.ncells = cells;
+    h->level_delta = delta;
+    destroy_graphs(h);
+    return SPH_OK;
+}
+
+// Mean device time of one forces-only evaluation (after one untimed one that
+// lets the radius guess settle on the previous smoothing lengths).
+int time_forces(sph_handle *h, int reps, double *ms) {
+    int rc = ensure_graphs(h);
+    if (rc) return rc;
+    if (!h->ev[0])
+        for (auto &e : h->ev) CUDA_TRY(cudaEventCreate(&e));
+    CUDA_TRY(cudaGraphLaunch(h->g_forces, h->stream));
+    CUDA_TRY(cudaEventRecord(h->ev[0], h->stream));
+    for (int r = 0; r < reps; r++) CUDA_TRY(cudaGraphLaunch(h->g_forces, h->stream));
+    CUDA_TRY(cudaEventRecord(h->ev[1], h->stream));
+    CUDA_TRY(cudaEventSynchronize(h->ev[1]));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
+    *ms = t / reps;
+    return check_flags(h);
+}
+
+std::string tune_cache_path() {
+    if (const char *p = std::getenv("SPHGPU_TUNE_CACHE")) return p;
+    const char *home = std::getenv("HOME");
+    return std::string(home ? home : "/tmp") + "/.cache/sphgpu/tune.txt";
+}
+
+struct TuneChoice {
+    float theta = 0.5f, hgrow = 1.04f;
+    int delta = 0;
+    double ms = 0.0;
+};
+
+std::string tune_key(const sph_handle *h, const char *dist) {
+    std::ostringstream o;
+    const int nb = (int)std::lround(2.0 * std::log2((double)std::max<int64_t>(h->n, 1)));
+    o << "nb=" << nb << " k=" << h->k << " form=" << h->mode << " sims=" << (h->nsims > 1 ? 2 : 1)
+      << " dist=" << dist;
+    return o.str();
+}
+
+bool tune_cache_get(const std::string &key, TuneChoice *c) {
+    std::ifstream f(tune_cache_path());
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        if (line.rfind("sphgpu-tune-v1 " + key + " ", 0) != 0) continue;
+        std::istringstream in(line.substr(16 + key.size()));
+        std::string tok;
+        while (in >> tok) {
+            const size_t eq = tok.find('=');
+            if (eq == std::string::npos) continue;
+            const std::string k = tok.substr(0, eq), v = tok.substr(eq + 1);
+            if (k == "theta") c->theta = std::stof(v);
+            else if (k == "hgrow") c->hgrow = std::stof(v);
+            else if (k == "delta") c->delta = std::stoi(v);
+            else if (k == "ms") c->ms = std::stod(v);
+        }
+        found = true;  // the last matching line wins
+    }
+    return found;
+}
+
+void tune_cache_put(const std::string &key, const TuneChoice &c) {
+    const std::string path = tune_cache_path();
+    std::error_code ec;
+    std::filesystem::create_directories(std::filesystem::path(path).parent_path(), ec);
+    std::ofstream f(path, std::ios::app);
+    if (!f) return;
+    f << "sphgpu-tune-v1 " << key << " theta=" << c.theta << " hgrow=" << c.hgrow << " delta=" << c.delta
+      << " ms=" << c.ms << "\n";
 }
 
 }  // namespace
@@ -649,6 +765,14 @@ int32_t sph_kernels_per_step(sph_handle *h) {
     return h->kernels_per_step;
 }
 
+int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches) {
+    if (!mismatches || n < 0) return fail(SPH_ERR_ARG, "bad argument");
+    long long m = 0;
+    if (div_selftest(n, seed, &m)) return fail(SPH_ERR_CUDA, "division self-check failed to run");
+    *mismatches = m;
+    return SPH_OK;
+}
+
 int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
@@ -656,6 +780,187 @@ int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops) {
         return fail(SPH_ERR_CUDA, "no CUDA device available");
     }
     if (probe_peaks(fp64_tflops, fp32_tflops)) return fail(SPH_ERR_CUDA, "throughput probe failed");
+    return SPH_OK;
+}
+
+int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_len) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (!h->uploaded || h->step != 0)
+        return fail(SPH_ERR_STATE, "sph_autotune runs on a freshly uploaded state (before the first step)");
+    const int64_t n = h->n;
+    double *d = h->d_io;
+    // keep the uploaded state (caller order) to restore it afterwards
+    launch_gather_state(h->ctx(), h->launch(), h->A, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, nullptr, nullptr,
+                        nullptr);
+    CUDA_TRY(cudaGetLastError());
+    int rc;
+    const KnnTune base = h->tune;
+    double ms0 = 0.0;
+    if ((rc = apply_levels(h, 0)) || (rc = time_forces(h, 1, &ms0))) return rc;
+    // distribution class from the spread of smoothing lengths
+    std::vector<double> hs(n);
+    CUDA_TRY(cudaMemcpyAsync(hs.data(), h->D.h, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    double m1 = 0.0, m2 = 0.0;
+    for (double v : hs) { m1 += v; m2 += v * v; }
+    m1 /= n;
+    const double cv = std::sqrt(std::max(m2 / n - m1 * m1, 0.0)) / std::max(m1, 1e-300);
+    const char *dist = cv < 0.2 ? "uniform" : cv < 0.6 ? "mild" : cv < 1.5 ? "clustered" : "extreme";
+    const std::string key = tune_key(h, dist);
+    TuneChoice best;
+    bool cached = use_cache && tune_cache_get(key, &best);
+    int trials = 0;
+    const int reps = std::max(1, std::min(3, (int)(150.0 / std::max(ms0, 1e-3))));
+    if (!cached) {
+        const float thetas[] = {0.35f, 0.5f, 0.7f, 1.0f};
+        const float hgrows[] = {1.02f, 1.04f, 1.08f};
+        best.ms = 1e300;
+        const int dmax = (cv < 0.6) ? 1 : 2;  // clustered data: dense regions want finer cells
+        for (int delta = -1; delta <= dmax; delta++) {
+            if ((rc = apply_levels(h, delta))) continue;
+            for (float th : thetas) {
+                h->tune.theta = th;
+                h->tune.hgrow = 1.04f;
+                destroy_graphs(h);
+                double ms = 0.0;
+                if ((rc = time_forces(h, reps, &ms))) return rc;
+                trials++;
+                if (ms < best.ms) { best.ms = ms; best.theta = th; best.delta = delta; best.hgrow = 1.04f; }
+            }
+        }
+        if ((rc = apply_levels(h, best.delta))) return rc;
+        h->tune.theta = best.theta;
+        for (float hg : hgrows) {
+            if (hg == 1.04f) continue;
+            h->tune.hgrow = hg;
+            destroy_graphs(h);
+            double ms = 0.0;
+            if ((rc = time_forces(h, reps, &ms))) return rc;
+            trials++;
+            if (ms < best.ms) { best.ms = ms; best.hgrow = hg; }
+        }
+        tune_cache_put(key, best);
+    }
+    h->tune = base;
+    h->tune.theta = best.theta;
+    h->tune.hgrow = best.hgrow;
+    if ((rc = apply_levels(h, best.delta))) return rc;
+    // back to the uploaded state
+    launch_scatter_state(h->ctx(), h->launch(), h->A, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, nullptr, nullptr,
+                         nullptr, false);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->evaluated = false;
+    if (report && report_len > 0) {
+        std::ostringstream o;
+        o << "{\"key\": \"" << key << "\", \"cached\": " << (cached ? "true" : "false") << ", \"trials\": " << trials
+          << ", \"theta\": " << best.theta << ", \"hgrow\": " << best.hgrow << ", \"level_delta\": " << best.delta
+          << ", \"ms_per_eval\": " << best.ms << ", \"ms_default\": " << ms0 << ", \"h_cv\": " << cv
+          << ", \"cache\": \"" << tune_cache_path() << "\"}";
+        strncpy(report, o.str().c_str(), (size_t)report_len - 1);
+        report[report_len - 1] = 0;
+    }
+    return SPH_OK;
+}
+
+// ---- checkpoint / resume: header, then the state arrays in storage order
+namespace {
+struct CkptHeader {
+    char magic[8];      // "SPHGPUCK"
+    uint32_t version;   // 1
+    uint32_t mode;
+    int64_t n;
+    int32_t nsims, k, step, level_delta;
+    uint64_t params_hash;
+    float theta, hgrow;  // search shape (the mixed form's sums follow its visiting order)
+};
+
+uint64_t fnv1a(const void *p, size_t len, uint64_t hsh = 1469598103934665603ull) {
+    const unsigned char *b = (const unsigned char *)p;
+    for (size_t i = 0; i < len; i++) { hsh ^= b[i]; hsh *= 1099511628211ull; }
+    return hsh;
+}
+
+uint64_t params_hash(const sph_handle *h) {
+    uint64_t x = fnv1a(h->params.data(), h->params.size() * sizeof(sph_params));
+    return fnv1a(h->offs.data(), h->offs.size() * sizeof(int64_t), x);
+}
+
+struct ArrayRef {
+    void *dev;
+    size_t bytes;
+};
+
+std::vector<ArrayRef> state_arrays(sph_handle *h) {
+    const size_t n = (size_t)h->n;
+    const PArrays &A = h->A;
+    return {{A.pos, 16 * n}, {A.vel, 16 * n}, {A.vp, 16 * n}, {A.acc, 16 * n}, {A.u, 8 * n},
+            {A.up, 8 * n},   {A.udot, 8 * n}, {A.id, 4 * n},  {A.hprev, 4 * n}};
+}
+}  // namespace
+
+int sph_save(sph_handle *h, const char *path) {
+    if (!h || !path) return fail(SPH_ERR_ARG, "null argument");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "nothing to save before sph_upload");
+    CkptHeader hd;
+    memset(&hd, 0, sizeof hd);
+    memcpy(hd.magic, "SPHGPUCK", 8);
+    hd.version = 1;
+    hd.mode = (uint32_t)h->mode;
+    hd.n = h->n;
+    hd.nsims = h->nsims;
+    hd.k = h->k;
+    hd.step = h->step;
+    hd.level_delta = h->level_delta;
+    hd.params_hash = params_hash(h);
+    hd.theta = h->tune.theta;
+    hd.hgrow = h->tune.hgrow;
+    std::ofstream f(path, std::ios::binary | std::ios::trunc);
+    if (!f) return fail(SPH_ERR_ARG, std::string("cannot write ") + path);
+    f.write((const char *)&hd, sizeof hd);
+    std::vector<char> buf;
+    for (const ArrayRef &a : state_arrays(h)) {
+        buf.resize(a.bytes);
+        CUDA_TRY(cudaMemcpyAsync(buf.data(), a.dev, a.bytes, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        f.write(buf.data(), (std::streamsize)a.bytes);
+    }
+    if (!f) return fail(SPH_ERR_ARG, std::string("write failed: ") + path);
+    return SPH_OK;
+}
+
+int sph_load(sph_handle *h, const char *path) {
+    if (!h || !path) return fail(SPH_ERR_ARG, "null argument");
+    Guard g(h);
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(SPH_ERR_ARG, std::string("cannot read ") + path);
+    CkptHeader hd;
+    f.read((char *)&hd, sizeof hd);
+    if (!f || memcmp(hd.magic, "SPHGPUCK", 8) != 0 || hd.version != 1)
+        return fail(SPH_ERR_ARG, "not a version-1 SPH checkpoint");
+    if (hd.n != h->n || hd.nsims != h->nsims || hd.k != h->k || hd.mode != (uint32_t)h->mode ||
+        hd.params_hash != params_hash(h))
+        return fail(SPH_ERR_ARG, "checkpoint was written by a handle with other parameters or sizes");
+    int rc;
+    if (hd.level_delta != h->level_delta && (rc = apply_levels(h, hd.level_delta))) return rc;
+    if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow) {
+        h->tune.theta = hd.theta;
+        h->tune.hgrow = hd.hgrow;
+        destroy_graphs(h);
+    }
+    std::vector<char> buf;
+    for (const ArrayRef &a : state_arrays(h)) {
+        buf.resize(a.bytes);
+        f.read(buf.data(), (std::streamsize)a.bytes);
+        if (!f) return fail(SPH_ERR_ARG, "truncated checkpoint");
+        CUDA_TRY(cudaMemcpyAsync(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    h->step = hd.step;
+    h->uploaded = true;
+    h->evaluated = false;
     return SPH_OK;
 }
 

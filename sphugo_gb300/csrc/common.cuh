@@ -97,6 +97,7 @@ struct Ctx {
     const SimDev *sims;
     SimDev *sims_rw;
     const int64_t *offs;   // nsims + 1 particle offsets
+    const int32_t *simidx; // per slot: its simulation (slot ranges never change); NULL for one simulation
     int nsims;
     int64_t n;
     int k;
@@ -104,6 +105,10 @@ struct Ctx {
 };
 
 // ---------------------------------------------------------------- helpers
+// The simulation owning slot i: binning keeps every simulation inside its own
+// slot range, so a static per-slot index answers with one load.
+__device__ __forceinline__ int sim_of(const Ctx &c, int64_t i) { return c.simidx ? __ldg(c.simidx + i) : 0; }
+
 __device__ __forceinline__ int find_sim(const int64_t *offs, int nsims, int64_t i) {
     int lo = 0, hi = nsims - 1;
     while (lo < hi) {
@@ -230,6 +235,7 @@ void launch_diagnostics(const Ctx &c, const Launch &L, const PArrays &A, const D
                         int64_t lo, int64_t hi, double *scratch);
 int knn_occupancy_blocks(int block, int cap, int mode);
 int probe_peaks(double *fp64_tflops, double *fp32_tflops);
+int div_selftest(int64_t n, uint64_t seed, long long *mismatches);
 // message returned by sph_last_error() on this thread
 void set_last_error(const std::string &msg);
 

@@ -31,7 +31,7 @@ void launch_prep(const Ctx &c, const Launch &L, bool) {
 __global__ void k_bbox(Ctx c, PArrays A, int pred) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        int s = find_sim(c.offs, c.nsims, i);
+        int s = sim_of(c, i);
         const SimDev &S = c.sims[s];
         if (S.periodic[0] && S.periodic[1]) continue;
         double2 p, vp;
@@ -78,7 +78,7 @@ void launch_grid(const Ctx &c, const Launch &L) {
 __global__ void k_bin(Ctx c, PArrays A, Tables T, int pred) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        int s = find_sim(c.offs, c.nsims, i);
+        int s = sim_of(c, i);
         const SimDev &S = c.sims[s];
         double2 p, vp;
         double up;
@@ -244,7 +244,7 @@ void launch_stable(const Ctx &c, const Launch &L, const Tables &T) {
 __global__ void k_permute(Ctx c, PArrays A, PArrays B, Tables T, int pred, int mixed) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        int s = find_sim(c.offs, c.nsims, i);
+        int s = sim_of(c, i);
         const SimDev &S = c.sims[s];
         const int64_t d = T.rank[i];  // destination slot (stable within the cell)
         double2 pos = A.pos[i], vel = A.vel[i];

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
     unsigned fl = 0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < a.c.n;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int s = find_sim(a.c.offs, a.c.nsims, q);
+        const int s = sim_of(a.c, q);
         const SimDev &S = a.c.sims[s];
         const double2 P = B.pos[q];
         const int32_t *nb = D.nbr + q * k;

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
 
     for (int64_t q = (int64_t)blockIdx.x * wpb + w; q < a.c.n; q += (int64_t)gridDim.x * wpb) {
         // Only FP32 / integer work below (FP64 would run 32-wide for one query).
-        const int s = find_sim(a.c.offs, a.c.nsims, q);
+        const int s = sim_of(a.c, q);
         const SimDev &S = a.c.sims[s];
         const float4 pr = B.rec[q];
         const float pxr = pr.x + pr.z, pyr = pr.y + pr.w;
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
     unsigned fl = 0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < a.c.n;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int s = find_sim(a.c.offs, a.c.nsims, q);
+        const int s = sim_of(a.c, q);
         const SimDev &S = a.c.sims[s];
         const double gamma = S.gamma;
         const double up = B.up[q];
@@ -480,10 +480,11 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             const double dk2 = nbr_d2(S, B, P, (uint32_t)nb[k - 1]);
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
+            const double yh = __drcp_rn(h);  // RN(1/h), shared by the k quotients d/h
             double acc = 0.0;
             for (int e = k - 1; e >= 0; e--) {
                 const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, (uint32_t)nb[e]));
-                const double x = __ddiv_rn(d, h);
+                const double x = div_rn_recip(d, h, yh);  // == __ddiv_rn(d, h)
                 if (x > 1.0 || x < 0.0) fl |= FLAG_Q_RANGE;
                 acc = __dadd_rn(acc, kf_exact(S.kernel, x));
                 dist[e] = make_double2(d, x);  // NNDists and q = NNDists/h for the force

@@ -98,7 +98,7 @@ constexpr int kMaxK = 128;
 __global__ void k_gather_nbrs(Ctx c, PArrays B, Derived D, int64_t *ids, double *dist, int32_t *img) {
     const int k = c.k;
     GRID_STRIDE(i, c.n) {
-        const int s = find_sim(c.offs, c.nsims, i);
+        const int s = sim_of(c, i);
         const SimDev &S = c.sims[s];
         const int64_t idq = B.id[i];
         const double2 P = B.pos[i];
@@ -252,6 +252,48 @@ int probe_peaks(double *fp64_tflops, double *fp32_tflops) {
     if (fp64_tflops) *fp64_tflops = d;
     if (fp32_tflops) *fp32_tflops = f;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// ---- self-check of the division sequences against the hardware division
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_div_selftest(int64_t n, uint64_t seed, unsigned long long *bad) {
+    unsigned long long nb = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t r1 = mix64(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(2 * i + 1));
+        const uint64_t r2 = mix64(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(2 * i + 2));
+        // random significands over 2^-40 .. 2^8, and quotients near rounding midpoints
+        const double b = __longlong_as_double((long long)((r1 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(983 + (r1 >> 58) % 48) << 52)));
+        double a = __longlong_as_double((long long)((r2 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(983 + (r2 >> 58) % 48) << 52)));
+        if (i & 1) {  // a = RN(b (q + ulp(q)/2)) for q in [1, 2): a/b lies next to a midpoint
+            const double q = __longlong_as_double((long long)((r2 & 0x000FFFFFFFFFFFFFull) | (1023ull << 52)));
+            a = __fma_rn(b, q, __dmul_rn(b, 0x1p-53));
+        }
+        const double ref = __ddiv_rn(a, b);
+        if (div_rn_recip(a, b, __drcp_rn(b)) != ref) nb++;
+        if (div3_rn(a) != __ddiv_rn(a, 3.0)) nb++;
+    }
+    if (nb) atomicAdd(bad, nb);
+}
+
+int div_selftest(int64_t n, uint64_t seed, long long *mismatches) {
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof *d) != cudaSuccess) return -1;
+    cudaMemset(d, 0, sizeof *d);
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_div_selftest<<<sms * 8, 256>>>(n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *mismatches = (long long)h;
+    return 0;
 }
 
 }  // namespace sphgpu

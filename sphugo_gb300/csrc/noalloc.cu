@@ -196,6 +196,7 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     c.sims = d_sims;
     c.sims_rw = d_sims;
     c.offs = d_offs;
+    c.simidx = nullptr;
     c.nsims = 1;
     c.n = n;
     c.k = p->k;

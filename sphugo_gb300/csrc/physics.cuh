@@ -11,6 +11,33 @@
 
 namespace sphgpu {
 
+// RN(a/3) in three FP64 instructions instead of a division. With
+// y = RN(1/3) = (1/3)(1 - 2^-54): q0 = RN(a y) is within one ulp of a/3, the
+// residual r = a - 3 q0 is a multiple of ulp(a/3) of at most three units and
+// so exact in the FMA, and q0 + r y = a/3 - (r/3) 2^-54 differs from a/3 by far
+// less than the distance from a/3 to any rounding midpoint (a/3 has a
+// fractional part of 0, 1/3 or 2/3 in units of its ulp), so RN(q0 + r y) is
+// RN(a/3). Valid for every finite a without underflow in r.
+__device__ __forceinline__ double div3_rn(double a) {
+    const double y = 0x1.5555555555555p-2;  // RN(1/3)
+    const double q0 = __dmul_rn(a, y);
+    const double r = __fma_rn(-3.0, q0, a);
+    return __fma_rn(r, y, q0);
+}
+
+// RN(a/b) given y = RN(1/b) (shared by many quotients with the same b):
+// q1 below is faithful (within one ulp of a/b), the residual a - b q1 is exact
+// in the FMA, and Markstein's theorem (y within half an ulp of 1/b, q1
+// faithful) makes RN(q1 + r1 y) the correctly rounded quotient. No
+// overflow/underflow for the operands used here (distances and their ratios).
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+    const double q0 = __dmul_rn(a, y);
+    const double r0 = __fma_rn(-b, q0, a);
+    const double q1 = __fma_rn(r0, y, q0);
+    const double r1 = __fma_rn(-b, q1, a);
+    return __fma_rn(r1, y, q1);
+}
+
 // sim/sph.go:258-276 Monahan2D and :284-304 Wendtland2D, reference rounding.
 __device__ __forceinline__ double kf_exact(int kernel, double q) {
     if (kernel == SPH_KERNEL_WENDLAND) {
@@ -23,7 +50,7 @@ __device__ __forceinline__ double kf_exact(int kernel, double q) {
         return __dadd_rn(__dsub_rn(__dmul_rn(qq, q), qq), 1.0 / 6.0);
     }
     double a = __dsub_rn(1.0, q);
-    return __ddiv_rn(__dmul_rn(__dmul_rn(a, a), a), 3.0);
+    return div3_rn(__dmul_rn(__dmul_rn(a, a), a));
 }
 __device__ __forceinline__ double kdf_exact(int kernel, double q) {
     if (kernel == SPH_KERNEL_WENDLAND) {

@@ -138,6 +138,13 @@ class SphConfig:
         return cfg
 
 
+def _autotune(h, use_cache: bool) -> dict:
+    import json
+    buf = C.create_string_buffer(1024)
+    L.check(L.load().sph_autotune(h, 1 if use_cache else 0, buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
 class ConfigError(Exception):
     """The error value of MakeConfigFromFile (reference message format)."""
 
@@ -215,6 +222,17 @@ class Simulation:
     def CalculateForces(self):
         """sim/sph.go:403-435."""
         L.check(L.load().sph_forces(self._h))
+
+    def Autotune(self, use_cache: bool = True) -> dict:
+        """Picks the neighbour search's launch shape for this workload (before the first step)."""
+        return _autotune(self._h, use_cache)
+
+    def Save(self, path: str):
+        """Checkpoint of the whole integrator state (resumes bit for bit)."""
+        L.check(L.load().sph_save(self._h, str(path).encode()))
+
+    def Load(self, path: str):
+        L.check(L.load().sph_load(self._h, str(path).encode()))
 
     def _diag(self, sim=-1):
         out = np.zeros(4)
@@ -312,6 +330,9 @@ class Ensemble:
 
     def Step(self, nsteps: int = 1):
         L.check(L.load().sph_step(self._h, int(nsteps)))
+
+    def Autotune(self, use_cache: bool = True) -> dict:
+        return _autotune(self._h, use_cache)
 
     def state(self) -> dict:
         names = ["x", "y", "vx", "vy", "u", "ax", "ay", "udot"]

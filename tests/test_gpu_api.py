@@ -46,3 +46,67 @@ def test_forms_share_neighbour_lists(gpu, precision):
     ib, db, mb = b.neighbours()
     assert np.array_equal(ia, ib) and np.array_equal(ma, mb) and np.array_equal(da, db)
     assert np.array_equal(a.derived()["h"], b.derived()["h"])
+
+
+@pytest.mark.parametrize("precision", ["Exact", "Mixed"])
+def test_autotune_keeps_results_and_caches(gpu, tmp_path, monkeypatch, precision):
+    monkeypatch.setenv("SPHGPU_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    a, b = _sim(12_000, precision), _sim(12_000, precision)
+    rep = a.Autotune(use_cache=False)
+    assert rep["cached"] is False and rep["trials"] >= 12 and rep["level_delta"] in (-1, 0, 1)
+    assert a.CurrentStep == 0
+    if precision == "Exact":  # exact sets and orders: tuning changes only speed
+        a.Step(3)
+        b.Step(3)
+        sa, sb = a.state(), b.state()
+        for k in sa:
+            assert np.array_equal(sa[k], sb[k]), k
+    else:  # exact sets; the FP32 sums may follow the search's visiting order
+        a.CalculateForces()
+        b.CalculateForces()
+        ia, da, _ = a.neighbours()
+        ib, db, _ = b.neighbours()
+        assert np.array_equal(ia, ib) and np.array_equal(da, db)
+        ra, rb = a.derived()["rho"], b.derived()["rho"]
+        assert np.allclose(ra, rb, rtol=1e-6, atol=0)
+    c = _sim(12_000, precision)
+    rep2 = c.Autotune(use_cache=True)
+    assert rep2["cached"] is True and rep2["theta"] == rep["theta"] and rep2["level_delta"] == rep["level_delta"]
+    assert (tmp_path / "tune.txt").read_text().count("sphgpu-tune-v1") == 1
+
+
+@pytest.mark.parametrize("precision", ["Exact", "Mixed"])
+def test_checkpoint_resume_is_bitwise(gpu, tmp_path, precision):
+    a = _sim(9000, precision)
+    a.Step(6)
+    b = _sim(9000, precision)
+    b.Step(3)
+    ck = tmp_path / "state.ck"
+    b.Save(ck)
+    c = _sim(9000, precision)
+    c.Load(ck)
+    assert c.CurrentStep == 3
+    c.Step(3)
+    sa, sc = a.state(), c.state()
+    for k in sa:
+        assert np.array_equal(sa[k], sc[k]), k
+
+
+def test_checkpoint_rejects_other_parameters(gpu, tmp_path):
+    a = _sim(3000)
+    a.Step(1)
+    a.Save(tmp_path / "s.ck")
+    b = _sim(3000, "Mixed")
+    with pytest.raises(L.SphError) as e:
+        b.Load(tmp_path / "s.ck")
+    assert e.value.code == L.SPH_ERR_ARG
+
+
+def test_division_sequences_are_correctly_rounded(gpu):
+    """The FP64 form replaces some IEEE divisions by FMA sequences that must
+    return the same bits (division by 3; a shared reciprocal with a Markstein
+    correction). Checked against the hardware division on 2e8 operand pairs,
+    half of them next to rounding midpoints."""
+    bad = C.c_int64(-1)
+    L.check(gpu.sph_selftest_division(200_000_000, 12345, C.byref(bad)))
+    assert bad.value == 0
