@@ -41,18 +41,56 @@ METRIC = "particle-steps/s on 1 GB300: mixed/batched vs plain FP64 GPU at stated
 TOLERANCES = {"neighbour_sets": "bit-exact", "fp64": "bit-exact", "fp64_fast": 1e-12,
               "mixed_rho": 1e-5, "mixed_accel_normalised": 1e-4, "mixed_udot_normalised": 1e-4}
 
-# Algorithmic work per particle and force evaluation at k = 32:
-# bytes for the streaming stages, FP64 flops (adds, multiplies, divisions and
-# square roots of the reference formulas, 1 flop each) for the FP64 stages.
-def algorithmic(k):
+# Algorithmic work per particle and force evaluation. Streaming stages count
+# HBM bytes. FP64 stages count the FP64 operations of the reference's own
+# formulas in FMA issue slots: an add, multiply or compare is one slot, a
+# correctly rounded division or square root costs `div` / `sqrt` slots as
+# priced by the device probe in the same run (the FP64 pipe's real cost of
+# those operations). Work the GPU form does beyond the formulas (recomputing
+# distances, reciprocals shared by two quotients) is not counted.
+#   density (sim/sph.go:306-323, :423-429, and the kNN's FP64 squared
+#     distance and final square root of each kept neighbour,
+#     sim/nearest-neighbour.go:64-80): per neighbour d2 = ((p+o)-q)^2 7 ops,
+#     sqrt, div (q = d/h), kernel F (4 ops for q < 0.5, 3 + one division by 3
+#     otherwise), 1 add; per particle h = sqrt, rho (3 + div), c (3 + sqrt),
+#     cA (2 + div).
+#   force (sim/sph.go:327-401 plus the leapfrog update :121-193):
+#     per neighbour dF (4 ops for q < 0.5, 2 otherwise), vAB 2, rAB 4, dot 3,
+#     (Pi + cA) + cB 2, x/y terms 2 x (2 + div + 1), du/dt term 2; per
+#     approaching pair (dot < 0) cAB, rhoAB, hAB 6, r2 3, mu 2 + div,
+#     Pi 5 + div; per particle the prefactor 3 + div, outputs 6, integrator 12.
+def algorithmic(k, div, sqrt, lo_frac, visc_frac):
+    kern_f = lo_frac * 4 + (1 - lo_frac) * (3 + div)
+    kern_df = lo_frac * 4 + (1 - lo_frac) * 2
+    dens = k * (7 + sqrt + div + kern_f + 1) + sqrt + (3 + div) + (3 + sqrt) + (2 + div)
+    force = k * (kern_df + 2 + 4 + 3 + 2 + 2 * (3 + div) + 2) + k * visc_frac * (6 + 3 + 2 + div + 5 + div) \
+        + (3 + div) + 6 + 12
     return {
-        "bin": {"bytes": 32 + 8, "unit": "GB/s"},
-        "scan": {"bytes": None, "unit": "GB/s"},  # per cell: 16 B, filled in below
-        "permute": {"bytes": 76 + 8 + 4 + 92, "unit": "GB/s"},
-        "knn_density": {"fp64_flops": 7 * (k + 1) + 8 * k + 12, "bytes": 16 + 4 * k + 8 * k + 56,
-                        "unit": "TFLOP/s"},
-        "force_integrate": {"fp64_flops": 34 * k + 30, "bytes": 80 + 4 * k + 8 * k, "unit": "TFLOP/s"},
+        "bin": {"bytes": 32 + 8},
+        "scan": {"bytes": None},  # per cell: 16 B, filled in below
+        "permute": {"bytes": 76 + 8 + 4 + 92},
+        "knn": {"bytes": 16 + 4 * k + 8},
+        "density": {"fp64_slots": dens, "bytes": 16 + 8 * k + 4 * k + 56},
+        "force_integrate": {"fp64_slots": force, "bytes": 80 + 4 * k + 8 * k},
     }
+
+
+def pair_statistics(sim, dth):
+    """Fraction of neighbour pairs with q < 0.5 and of approaching pairs
+    (v_AB . r_AB < 0, with VPred = Vel + VDot dth), which set the taken
+    branches of the kernel functions and of the viscosity term."""
+    import numpy as np
+    st = sim.state()
+    ids, dist, img = sim.neighbours()
+    h = dist[:, :1]
+    lo = float(np.mean(dist < 0.5 * h))
+    vpx, vpy = st["vx"] + st["ax"] * dth, st["vy"] + st["ay"] * dth
+    L = 1.0
+    ia, ib = img // 3 - 1, img % 3 - 1
+    rx = (st["x"][ids] - ia * L) - st["x"][:, None]
+    ry = (st["y"][ids] - ib * L) - st["y"][:, None]
+    dot = (vpx[ids] - vpx[:, None]) * rx + (vpy[ids] - vpy[:, None]) * ry
+    return lo, float(np.mean(dot < 0))
 
 
 def env_rank():
@@ -141,6 +179,18 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def ncu_traffic(kernel, form, n):
+    """DRAM bytes per launch of a stage's kernel from the committed ncu
+    summary (profiles/ncu_traffic.json), for the same form and size."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            tab = json.load(f)
+    except (OSError, ValueError):
+        return None
+    ent = tab.get(f"{kernel}/{form.lower()}/{n}")
+    return ent.get("dram_bytes_per_launch") if ent else None
 
 
 def measured_peaks():
@@ -268,7 +318,7 @@ def run_reference(args, dist):
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head_form != "Mixed" else "f32+f64", "data": "synthetic (seeded SplitMix64)",
         "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}",
                    "n": n, "k": K_NEIGH, "form": "reference tree search, FP64"},
         "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
@@ -307,10 +357,13 @@ def run_ours(args, dist):
     lib = L.load()
     n = args.n or N_DEFAULT
     K, W = max(1, args.steps), max(3, args.warmup)
-    fp64_pk, fp32_pk = C.c_double(0), C.c_double(0)
-    L.check(lib.sph_probe_peaks(C.byref(fp64_pk), C.byref(fp32_pk)))
+    fp64_pk, fp32_pk, div_cost, sqrt_cost = C.c_double(0), C.c_double(0), C.c_double(0), C.c_double(0)
+    L.check(lib.sph_probe_peaks(C.byref(fp64_pk), C.byref(fp32_pk), C.byref(div_cost), C.byref(sqrt_cost)))
 
     form = {"exact": "Exact", "fast": "Fast", "mixed": "Mixed"}[args.form]
+    form_name = {"Exact": "SPH_PREC_FP64 (bit-exact)", "Fast": "SPH_PREC_FP64_FAST (FMA, <=1e-12)",
+                 "Mixed": "SPH_PREC_MIXED (FP32 relative-coordinate Kahan sums, FP64 kNN decisions/h/integrator)"}[form]
+    head_form = form
     sim = make_sim(n, form, SEED + 1000 * dist.rank)
     tune_report = sim.tune_report
     sim.Step(W)
@@ -325,29 +378,36 @@ def run_ours(args, dist):
     value = n * K * dist.world / (ms_max / 1e3)
 
     stages = profile(sim, 3)
-    work = algorithmic(K_NEIGH)
+    lo_frac, visc_frac = pair_statistics(sim, DT / 2)
+    work = algorithmic(K_NEIGH, div_cost.value, sqrt_cost.value, lo_frac, visc_frac)
     ncells = 4 ** 10  # auto level for N = 2^20
-    dom = max(stages, key=stages.get)
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs")
+    slot_peak = fp64_pk.value / 2 * 1e3  # G FP64 FMA issue slots per second
     roof = {}
     for st, t in stages.items():
         w = work[st]
         entry = {"ms": t}
-        if "fp64_flops" in w:
-            entry.update(bound="fp64", unit="TFLOP/s", achieved=w["fp64_flops"] * n / (t * 1e-3) / 1e12,
-                         peak=fp64_pk.value)
+        if "fp64_slots" in w and form != "Mixed":
+            entry.update(bound="fp64", unit="G FP64-slot/s", achieved=w["fp64_slots"] * n / (t * 1e-3) / 1e9,
+                         peak=slot_peak)
         else:
             b = w["bytes"] * n if w["bytes"] else 16 * ncells
             entry.update(bound="hbm", unit="GB/s", achieved=b / (t * 1e-3) / 1e9, peak=hbm_peak)
         if entry.get("peak"):
             entry["frac"] = entry["achieved"] / entry["peak"]
         roof[st] = entry
+    dom = max(stages, key=stages.get)
     d = roof[dom]
+    traffic = ncu_traffic(dom, form, n)
     roofline = {"kernel": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
-                "unit": d["unit"], "frac": d.get("frac"), "traffic": None,
-                "peak_source": ("FP64 FMA probe run by this bench (MEASURED_PEAKS.json has no FP64 figure)"
-                                if d["bound"] == "fp64" else "MEASURED_PEAKS.json hbm_gbs"),
+                "unit": d["unit"], "frac": d.get("frac"), "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                "peak_source": ("FP64 FMA issue rate from the device probe run by this bench (2 flops per slot; "
+                                "MEASURED_PEAKS.json has no FP64 figure)" if d["bound"] == "fp64"
+                                else "MEASURED_PEAKS.json hbm_gbs"),
+                "fp64_costs": {"div_slots": div_cost.value, "sqrt_slots": sqrt_cost.value,
+                               "q_below_half": lo_frac, "approaching_pairs": visc_frac},
                 "stages": roof}
 
     dt, h2d, d2h = e2e_run(sim, max(3, K // 2))
@@ -389,13 +449,14 @@ def run_ours(args, dist):
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": dist.world, "steps": K,
             "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 uniform blast)",
-            "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}, plain FP64",
-                       "n": n, "k": K_NEIGH, "form": "SPH_PREC_FP64 (bit-exact)", "parallelism": "replicas",
+            "vs_baseline": None, "dtype": "f64" if head_form != "Mixed" else "f32+f64", "data": "synthetic (seeded SplitMix64 uniform blast)",
+            "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}, {head_form.lower()} form",
+                       "n": n, "k": K_NEIGH, "form": form_name, "parallelism": "replicas",
                        "l2": "inputs larger than L2 (state + neighbour lists > 1 GB)"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": kernels * K, "kernels_per_step": kernels,
             "roofline": roofline, "cpu_baseline": cpu, "tolerances": TOLERANCES,
-            "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value}, "forms": extras,
+            "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value,
+                            "fp64_div_slots": div_cost.value, "fp64_sqrt_slots": sqrt_cost.value}, "forms": extras,
             "tune": tune_report,
         }
         print(json.dumps(line), flush=True)

@@ -130,7 +130,7 @@ int sph_save(sph_handle *h, const char *path);
 int sph_load(sph_handle *h, const char *path);
 
 /* ---- measurement (no reference counterpart) ---- */
-#define SPH_NUM_STAGES 5   /* bin (incl. prep/bbox), scan, permute, knn+density, force+integrate */
+#define SPH_NUM_STAGES 6   /* bin (incl. prep/bbox), scan, permute, knn, density, force+integrate */
 /* sph_step with the device time between CUDA events recorded on the
  * handle's stream before the first and after the last step, in ms. */
 int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms);
@@ -153,8 +153,11 @@ int32_t sph_kernels_per_step(sph_handle *h);
  * report (may be NULL) receives a one-line JSON summary. */
 int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_len);
 /* Arithmetic throughput probe on the current device: FP64 FMA and FP32 FMA
- * in TFLOP/s (2 flops per FMA), from independent FMA chains. */
-int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops);
+ * in TFLOP/s (2 flops per FMA), from independent FMA chains, and the cost of
+ * one correctly rounded FP64 division and square root in FP64 FMA issue
+ * slots (time per operation / time per FMA, at full occupancy). Any output
+ * pointer may be NULL. */
+int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost);
 
 /* ---- allocation-free neighbour search and density ----
  * No counterpart in the reference. For callers that cannot call cudaMalloc

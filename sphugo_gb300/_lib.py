@@ -45,8 +45,8 @@ EXPORTS = [
 ]
 NOALLOC_MAX_N = 8192
 NOALLOC_MAX_K = 32
-NUM_STAGES = 5
-STAGES = ["bin", "scan", "permute", "knn_density", "force_integrate"]
+NUM_STAGES = 6
+STAGES = ["bin", "scan", "permute", "knn", "density", "force_integrate"]
 
 
 class SphParams(C.Structure):
@@ -141,7 +141,7 @@ def load() -> C.CDLL:
     L.sph_step_profiled.argtypes = [vp, C.c_int32, dp]
     L.sph_kernels_per_step.argtypes = [vp]
     L.sph_kernels_per_step.restype = C.c_int32
-    L.sph_probe_peaks.argtypes = [dp, dp]
+    L.sph_probe_peaks.argtypes = [dp, dp, dp, dp]
     L.sph_autotune.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
     L.sph_save.argtypes = [vp, C.c_char_p]
     L.sph_selftest_division.argtypes = [C.c_int64, C.c_uint64, i64p]

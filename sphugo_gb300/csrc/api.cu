@@ -229,8 +229,10 @@ void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) 
     mark(3);
     launch_knn(c, L, h->B, h->D, h->T, h->mode, h->tune);
     mark(4);
-    launch_force(c, L, h->B, h->A, h->D, h->mode, integrate);
+    launch_density(c, L, h->B, h->D, h->mode);
     mark(5);
+    launch_force(c, L, h->B, h->A, h->D, h->mode, integrate);
+    mark(6);
 }
 
 int count_kernel_nodes(cudaGraph_t g) {
@@ -773,13 +775,13 @@ int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches) {
     return SPH_OK;
 }
 
-int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops) {
+int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
         cudaGetLastError();
         return fail(SPH_ERR_CUDA, "no CUDA device available");
     }
-    if (probe_peaks(fp64_tflops, fp32_tflops)) return fail(SPH_ERR_CUDA, "throughput probe failed");
+    if (probe_peaks(fp64_tflops, fp32_tflops, div_cost, sqrt_cost)) return fail(SPH_ERR_CUDA, "throughput probe failed");
     return SPH_OK;
 }
 

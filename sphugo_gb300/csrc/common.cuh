@@ -219,6 +219,7 @@ struct KnnTune {
 void knn_init_attrs();
 void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D,
                 const Tables &T, int mode, const KnnTune &tune);
+void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode);
 void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays &A,
                   const Derived &D, int mode, bool integrate);
 
@@ -234,7 +235,7 @@ void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &A, c
 void launch_diagnostics(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D,
                         int64_t lo, int64_t hi, double *scratch);
 int knn_occupancy_blocks(int block, int cap, int mode);
-int probe_peaks(double *fp64_tflops, double *fp32_tflops);
+int probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost);
 int div_selftest(int64_t n, uint64_t seed, long long *mismatches);
 // message returned by sph_last_error() on this thread
 void set_last_error(const std::string &msg);

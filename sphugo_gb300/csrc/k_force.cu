@@ -83,8 +83,10 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                                                __dmul_rn(__dmul_rn(S.beta, mu), mu)), rhoab);
                 }
                 const double sum3 = __dadd_rn(__dadd_rn(piab, ca), dj.w);
-                ax = __dadd_rn(ax, __ddiv_rn(__dmul_rn(__dmul_rn(rabx, sum3), drk), d));
-                ay = __dadd_rn(ay, __ddiv_rn(__dmul_rn(__dmul_rn(raby, sum3), drk), d));
+                // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
+                const double yd = __drcp_rn(d);
+                ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
+                ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
                 ed = __dadd_rn(ed, __dmul_rn(dot, drk));
             }
             const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));

@@ -597,6 +597,10 @@ static void run_knn(const KnnArgs &args, const Launch &L, const KnnTune &tune) {
     else if (nr == 2) k_knn<MODE, 2><<<grid, kKnnBlock, smem, L.stream>>>(args);
     else if (nr == 4) k_knn<MODE, 4><<<grid, kKnnBlock, smem, L.stream>>>(args);
     else k_knn<MODE, 8><<<grid, kKnnBlock, smem, L.stream>>>(args);
+}
+
+template <int MODE>
+static void run_density(const KnnArgs &args, const Launch &L) {
     const int64_t dneed = (args.c.n + 255) / 256;
     const int dgrid = (int)std::max<int64_t>(1, std::min<int64_t>(dneed, (int64_t)L.sms * 8));
     k_density<MODE><<<dgrid, 256, 0, L.stream>>>(args);
@@ -614,6 +618,16 @@ void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &
     if (mode == MODE_EXACT64) run_knn<MODE_EXACT64>(a, L, tune);
     else if (mode == MODE_FAST64) run_knn<MODE_FAST64>(a, L, tune);
     else run_knn<MODE_MIXED>(a, L, tune);
+}
+
+void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode) {
+    KnnArgs a{};
+    a.c = c;
+    a.B = B;
+    a.D = D;
+    if (mode == MODE_EXACT64) run_density<MODE_EXACT64>(a, L);
+    else if (mode == MODE_FAST64) run_density<MODE_FAST64>(a, L);
+    else run_density<MODE_MIXED>(a, L);
 }
 
 }  // namespace sphgpu

@@ -219,7 +219,36 @@ __global__ void k_fma_chains(T *out, int iters, T a, T b) {
     if (s == (T)12345.678) out[0] = s;  // keeps the chains live
 }
 
-int probe_peaks(double *fp64_tflops, double *fp32_tflops) {
+// Dependent chains of correctly rounded divisions / square roots, eight per
+// thread, to price them against the FMA chains above at full occupancy.
+__global__ void k_div_chains(double *out, int iters, double a, double) {
+    double x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = 1.0 + threadIdx.x * 1e-6 + i * 1e-3;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = __ddiv_rn(a, x[i]);
+    }
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    if (s == 12345.678) out[0] = s;
+}
+__global__ void k_sqrt_chains(double *out, int iters, double a, double) {
+    double x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = a + threadIdx.x * 1e-3 + i;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = __dsqrt_rn(x[i]);
+    }
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    if (s == 12345.678) out[0] = s;
+}
+
+int probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -229,6 +258,7 @@ int probe_peaks(double *fp64_tflops, double *fp32_tflops) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const int blocks = sms * 8, threads = 256;
+    // seconds per operation per thread-chain element (best of three)
     auto run = [&](auto kern, auto a, auto b, int iters) {
         kern<<<blocks, threads>>>((decltype(a) *)buf, 8, a, b);
         cudaDeviceSynchronize();
@@ -242,15 +272,19 @@ int probe_peaks(double *fp64_tflops, double *fp32_tflops) {
             cudaEventElapsedTime(&ms, e0, e1);
             best = ms < best ? ms : best;
         }
-        return 2.0 * blocks * threads * 8.0 * iters / (best * 1e-3) / 1e12;
+        return (double)best * 1e-3 / ((double)blocks * threads * 8.0 * iters);
     };
-    double d = run(k_fma_chains<double>, 0.999999, 1e-7, 2000);
-    double f = run(k_fma_chains<float>, 0.999999f, 1e-7f, 20000);
+    const double t_dfma = run(k_fma_chains<double>, 0.999999, 1e-7, 2000);
+    const double t_ffma = run(k_fma_chains<float>, 0.999999f, 1e-7f, 20000);
+    const double t_ddiv = run(k_div_chains, 1.0000001, 0.0, 100);
+    const double t_dsqrt = run(k_sqrt_chains, 3.0, 0.0, 100);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(buf);
-    if (fp64_tflops) *fp64_tflops = d;
-    if (fp32_tflops) *fp32_tflops = f;
+    if (fp64_tflops) *fp64_tflops = 2.0 / t_dfma / 1e12;
+    if (fp32_tflops) *fp32_tflops = 2.0 / t_ffma / 1e12;
+    if (div_cost) *div_cost = t_ddiv / t_dfma;
+    if (sqrt_cost) *sqrt_cost = t_dsqrt / t_dfma;
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

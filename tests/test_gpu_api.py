@@ -32,9 +32,11 @@ def test_timed_and_profiled_steps(gpu):
 
 
 def test_probe_peaks(gpu):
-    d, f = C.c_double(), C.c_double()
-    L.check(gpu.sph_probe_peaks(C.byref(d), C.byref(f)))
+    d, f, dv, sq = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    L.check(gpu.sph_probe_peaks(C.byref(d), C.byref(f), C.byref(dv), C.byref(sq)))
     assert 0.1 < d.value < 20 and f.value > 10 * d.value
+    assert 1.0 < dv.value < 100 and 1.0 < sq.value < 100
+    L.check(gpu.sph_probe_peaks(C.byref(d), None, None, None))
 
 
 @pytest.mark.parametrize("precision", ["Fast", "Mixed"])
