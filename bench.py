@@ -378,6 +378,7 @@ def run_ours(args, dist):
     value = n * K * dist.world / (ms_max / 1e3)
 
     stages = profile(sim, 3)
+    nq, ndef = sim.search_stats()
     lo_frac, visc_frac = pair_statistics(sim, DT / 2)
     work = algorithmic(K_NEIGH, div_cost.value, sqrt_cost.value, lo_frac, visc_frac)
     ncells = 4 ** 10  # auto level for N = 2^20
@@ -423,7 +424,7 @@ def run_ours(args, dist):
             t = timed(s2, K)
             extras[{"Fast": "fp64_fast", "Mixed": "mixed"}[form]] = {
                 "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3),
-                "tune": s2.tune_report}
+                "tune": s2.tune_report, "search_deferred": s2.search_stats()[1]}
             s2.close()
         extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
         ens = {}
@@ -458,6 +459,8 @@ def run_ours(args, dist):
             "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value,
                             "fp64_div_slots": div_cost.value, "fp64_sqrt_slots": sqrt_cost.value}, "forms": extras,
             "tune": tune_report,
+            "search": {"queries": nq, "deferred_to_per_query": ndef,
+                       "path": "group tiles + per-query for deferred" if ndef < nq else "per-query"},
         }
         print(json.dumps(line), flush=True)
     return 0

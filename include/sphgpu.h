@@ -129,6 +129,29 @@ int64_t sph_num_particles(const sph_handle *h);
 int sph_save(sph_handle *h, const char *path);
 int sph_load(sph_handle *h, const char *path);
 
+/* Append particles to a single simulation, as Step does with the particles
+ * its sources spawn (sim/sph.go:71-85: Spawn(t) then append to
+ * Root.Particles). They take caller indices n .. n+count-1, zero
+ * acceleration and du/dt, and join the binning at the next evaluation; the
+ * arrays grow like a Go slice (x1.5) and the step graphs are captured again.
+ * vx, vy, u may be NULL (zero); z (may be NULL) gives their draw keys
+ * (Particle.Z) for sph_render. */
+int sph_append(sph_handle *h, int64_t count, const double *x, const double *y, const double *vx,
+               const double *vy, const double *u, const int64_t *z);
+
+/* ---- frames (sim/animator.go:55-103 CurrentFrame, gx/graphics.go) ----
+ * Draw keys per caller index (Particle.Z; n values, NULL = caller order):
+ * disks are painted in descending Z (the reference sorts by -Z), ties by
+ * caller index, so the smallest Z ends on top. */
+int sph_set_draw_keys(sph_handle *h, const int64_t *z);
+/* Renders the current state into rgba (width*height*4 bytes, NRGBA, row y =
+ * Pos.Y*height from the top): black background, a disk of radius 4 pixels per
+ * particle at (Pos.X*width, Pos.Y*height) with the reference's float32 pixel
+ * test, coloured by ParaRamp(min(rho/(m N 10)*256, 255)) from the densities
+ * of the last force evaluation (0 for particles that have none yet). The
+ * reference's canvas is 1280 x 720. Single simulations only. */
+int sph_render(sph_handle *h, int32_t width, int32_t height, uint8_t *rgba);
+
 /* ---- measurement (no reference counterpart) ---- */
 #define SPH_NUM_STAGES 6   /* bin (incl. prep/bbox), scan, permute, knn, density, force+integrate */
 /* sph_step with the device time between CUDA events recorded on the
@@ -140,6 +163,16 @@ int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms);
 int sph_step_profiled(sph_handle *h, int32_t nsteps, double stage_ms[SPH_NUM_STAGES]);
 /* Kernel launches of one regular step (graph kernel nodes). */
 int32_t sph_kernels_per_step(sph_handle *h);
+/* Neighbour search path (no reference counterpart): 1 (default) = one warp
+ * per group of 32 consecutive particles scanning a shared-memory tile of
+ * candidate records, with the queries it cannot settle finished by the
+ * per-query search; 0 = per-query search for every particle. The neighbour
+ * sets and every FP64 result are identical; the mixed form's FP32 sums may
+ * differ in the last bits (they follow the list order). */
+int sph_set_search(sph_handle *h, int32_t tiles);
+/* Queries of the last force evaluation and how many of them the group-tile
+ * search left to the per-query search (all of them with tiles off). */
+int sph_search_stats(sph_handle *h, int64_t *queries, int64_t *deferred);
 /* Autotuner (no reference counterpart): on a freshly uploaded state (before
  * the first step) it times forces-only evaluations over a small grid of the
  * neighbour search's shape (cell side / search radius factor, radius-guess
@@ -270,13 +303,15 @@ int64_t sph_config_start_count(const sph_config *cfg);
  * (sim/config-parser.go:58-80): the generator is reseeded with 12345678 at
  * each spawner, as the reference reseeds math/rand; E = 0.01, v = 0.
  * Arrays hold sph_config_start_count() entries; vx, vy, u may be NULL. */
-int sph_config_spawn(const sph_config *cfg, double *x, double *y, double *vx, double *vy, double *u);
+int sph_config_spawn(const sph_config *cfg, double *x, double *y, double *vx, double *vy, double *u,
+                     int64_t *z);
 /* PointSource.Spawn(t) (sim/config-parser.go:82-102): returns how many
  * particles the source emits at time t (int(deltaT / cooldown)), advances its
  * last_spawned clock, and when x/y are not NULL fills them (origin +- 0.01
- * uniform, seeded by seed) with u = 0.002 and v = 0. */
+ * uniform, seeded by seed) with u = 0.002, v = 0 and draw keys z (may be
+ * NULL). */
 int64_t sph_point_source_spawn(sph_point_source *src, double t, uint64_t seed, double *x, double *y,
-                               double *vx, double *vy, double *u);
+                               double *vx, double *vy, double *u, int64_t *z);
 
 #ifdef __cplusplus
 }

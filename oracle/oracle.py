@@ -84,6 +84,10 @@ def lib():
         for f in (L.orc_kernel_f, L.orc_kernel_df):
             f.argtypes = [C.c_int, C.c_double]
             f.restype = C.c_double
+        L.orc_append.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
+        L.orc_draw_order.argtypes = [C.c_int64, i64p, i64p]
+        u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+        L.orc_render.argtypes = [C.c_int64, dp, dp, dp, C.c_double, i64p, C.c_int, C.c_int, u8p]
         for f in (L.orc_kernel_fpref, L.orc_kernel_dfpref):
             f.argtypes = [C.c_int]
             f.restype = C.c_double
@@ -139,6 +143,17 @@ class OracleSim:
         if rc:
             raise RuntimeError(f"oracle step failed: status {rc}")
 
+    def append(self, x, y, vx=None, vy=None, u=None):
+        """Particles spawned during the run (sim/sph.go:71-85)."""
+        m = len(x)
+        z = np.zeros(m)
+        rc = lib().orc_append(self._h, m, _c(x), _c(y), _c(z if vx is None else vx), _c(z if vy is None else vy),
+                              _c(z if u is None else u))
+        if rc:
+            raise RuntimeError(f"oracle append failed: status {rc}")
+        self.n += m
+        self.params.n = self.n
+
     def forces(self):
         rc = lib().orc_forces(self._h)
         if rc:
@@ -187,6 +202,22 @@ class OracleSim:
         out = np.empty(3)
         lib().orc_diagnostics(self._h, out)
         return out
+
+
+def draw_order(z):
+    """Painting order of sim/animator.go:65-70 (QuickSort by -Z)."""
+    z = np.ascontiguousarray(z, np.int64)
+    order = np.empty(len(z), np.int64)
+    lib().orc_draw_order(len(z), z, order)
+    return order
+
+
+def render(x, y, rho, mass, order, width=1280, height=720):
+    """sim/animator.go:55-103 CurrentFrame as (height, width, 4) NRGBA bytes."""
+    out = np.empty((height, width, 4), np.uint8)
+    lib().orc_render(len(x), _c(x), _c(y), _c(rho), float(mass), np.ascontiguousarray(order, np.int64),
+                     width, height, out)
+    return out
 
 
 def knn_exact(params: Params, x, y, brute=False):

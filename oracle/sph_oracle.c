@@ -847,3 +847,115 @@ int orc_tree_count_outside(const double *x, const double *y, int n) {
     orc_destroy(s);
     return out;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Particles spawned during a run (sim/sph.go:71-85: Spawn then append to
+ * Root.Particles). Go zero values for everything the spawner does not set. */
+int orc_append(orc_sim *s, int n_new, const double *x, const double *y, const double *vx,
+               const double *vy, const double *u) {
+    if (!s || n_new < 0) return ORC_ERR_ARG;
+    if (n_new == 0) return ORC_OK;
+    const int n0 = s->p.n, n1 = n0 + n_new, k = s->p.k;
+    double *bd = (double *)calloc((size_t)n1 * k * 3, sizeof(double));
+    int32_t *bi = (int32_t *)calloc((size_t)n1 * k * 2, sizeof(int32_t));
+    P *ps = (P *)calloc((size_t)n1, sizeof(P));
+    memcpy(ps, s->ps, (size_t)n0 * sizeof(P));
+    memcpy(bd, s->blk_d, (size_t)n0 * k * 3 * sizeof(double));
+    memcpy(bi, s->blk_i, (size_t)n0 * k * 2 * sizeof(int32_t));
+    for (int i = 0; i < n0; i++) {  /* blocks keep their offsets */
+        P *q = &ps[i];
+        q->nnd = bd + (q->nnd - s->blk_d);
+        q->nnx = bd + (q->nnx - s->blk_d);
+        q->nny = bd + (q->nny - s->blk_d);
+        q->nn = bi + (q->nn - s->blk_i);
+        q->nimg = bi + (q->nimg - s->blk_i);
+    }
+    for (int i = n0; i < n1; i++) {
+        P *q = &ps[i];
+        const int a = i - n0;
+        q->x = x[a]; q->y = y[a];
+        q->vx = vx ? vx[a] : 0; q->vy = vy ? vy[a] : 0;
+        q->e = u ? u[a] : 0;
+        q->id = i;
+        q->nnd = bd + (size_t)i * k * 3;
+        q->nnx = q->nnd + k;
+        q->nny = q->nnd + 2 * k;
+        q->nn = bi + (size_t)i * k * 2;
+        q->nimg = q->nn + k;
+        for (int b = 0; b < k; b++) q->nn[b] = -1;
+    }
+    free(s->ps); free(s->blk_d); free(s->blk_i);
+    s->ps = ps; s->blk_d = bd; s->blk_i = bi;
+    s->p.n = n1;
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* sim/heap.go:229-268 QuickSort / partitionQS on particle indices with the
+ * comparison value -Z (sim/animator.go:65-70). */
+static void quicksort_negz(int64_t *ps, int64_t len, const int64_t *z) {
+    while (len > 0) {
+        int64_t i = 0, j = len - 2;
+        const int64_t pivot = -z[ps[len - 1]];
+        while (i < j) {
+            while (i < j && -z[ps[i]] <= pivot) i++;
+            while (i < j && -z[ps[j]] > pivot) j--;
+            if (-z[ps[i]] > -z[ps[j]]) { int64_t t = ps[i]; ps[i] = ps[j]; ps[j] = t; }
+        }
+        if (-z[ps[i]] > pivot) { int64_t t = ps[i]; ps[i] = ps[len - 1]; ps[len - 1] = t; }
+        else i = len - 1;
+        quicksort_negz(ps, i, z);          /* left: ps[:i] */
+        ps += i + 1;                        /* right: ps[i+1:] */
+        len -= i + 1;
+    }
+}
+
+void orc_draw_order(int64_t n, const int64_t *z, int64_t *order) {
+    for (int64_t i = 0; i < n; i++) order[i] = i;
+    quicksort_negz(order, n, z);
+}
+
+/* gx/graphics.go:156-164 ParaRamp */
+static void para_ramp(int index, uint8_t *rgb) {
+    const double x = (double)index;
+    const double r = fmin(215, fmax(0, -fabs((x - 60) * 31 / 17 - 232) + 245));
+    const double g = fmin(190, fmax(0, -fabs(x * 31 / 17 - 232) + 245));
+    const double b = fmin(215, fmax(0, -fabs((x + 70) * 31 / 17 - 232) + 245));
+    rgb[0] = (uint8_t)r; rgb[1] = (uint8_t)g; rgb[2] = (uint8_t)b;
+}
+
+/* sim/animator.go:55-103 CurrentFrame: black canvas, then for each particle in
+ * `order` a disk of radius 4 (gx/graphics.go:90-107 DrawDisk, float32 pixel
+ * test) coloured by ParaRamp(uint8(min(rho/(m*N*10)*256, 255))). x, y, rho in
+ * caller order. */
+void orc_render(int64_t n, const double *x, const double *y, const double *rho, double mass,
+                const int64_t *order, int W, int H, uint8_t *rgba) {
+    for (int64_t p = 0; p < (int64_t)W * H; p++) {
+        rgba[4 * p] = 0; rgba[4 * p + 1] = 0; rgba[4 * p + 2] = 0; rgba[4 * p + 3] = 255;
+    }
+    const double n10 = (double)(n * 10);
+    for (int64_t o = 0; o < n; o++) {
+        const int64_t i = order[o];
+        const float cx = (float)x[i] * (float)W;
+        const float cy = (float)y[i] * (float)H;
+        const double cf = rho[i] / (mass * n10) * 256;
+        const double mn = cf > 255 ? 255 : cf;  /* math.Min keeps a NaN; uint8(NaN) = 0 */
+        const int idx = mn >= 0 ? (int)mn : 0;
+        uint8_t rgb[3];
+        para_ramp(idx, rgb);
+        const float radius = 4;
+        const double xa = floor((double)(cx - radius)), xb = ceil((double)(cx + radius));
+        const double ya = floor((double)(cy - radius)), yb = ceil((double)(cy + radius));
+        for (double fx = xa; fx <= xb; fx++) {
+            for (double fy = ya; fy <= yb; fy++) {
+                const int px = (int)fx, py = (int)fy;
+                const float dx = (float)px - cx, dy = (float)py - cy;
+                const float r2 = dx * dx + dy * dy;
+                if (r2 <= radius * radius && px >= 0 && px < W && py >= 0 && py < H) {
+                    uint8_t *d = rgba + 4 * ((int64_t)py * W + px);
+                    d[0] = rgb[0]; d[1] = rgb[1]; d[2] = rgb[2]; d[3] = 255;
+                }
+            }
+        }
+    }
+}

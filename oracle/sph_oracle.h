@@ -15,6 +15,10 @@
  *   - AccelerationAndEDot2D                           sim/sph.go:327-401
  *   - Step (leapfrog, periodic wrap, reflections)     sim/sph.go:64-198
  *   - TotalEnergy / TotalDensity / TotalMomentum      sim/sph.go:441-463
+ *   - sources appending particles during a run        sim/sph.go:71-85
+ *   - the animator's frame (QuickSort by -Z, disks,   sim/animator.go:55-103,
+ *     ParaRamp)                                       sim/heap.go:229-268,
+ *                                                     gx/graphics.go:90-164
  * and adds an independent exact kNN (grid search, ties broken by
  * (squared distance, particle id, image code)) that defines the neighbour
  * sets the GPU path must reproduce bit for bit.
@@ -115,6 +119,16 @@ double orc_kernel_f(int kernel, double q);
 double orc_kernel_df(int kernel, double q);
 double orc_kernel_fpref(int kernel);
 double orc_kernel_dfpref(int kernel);
+
+/* Particles spawned during a run (sim/sph.go:71-85), appended with ids n.. */
+int orc_append(orc_sim *s, int n_new, const double *x, const double *y, const double *vx,
+               const double *vy, const double *u);
+
+/* Frames (sim/animator.go:55-103): draw order by the reference's QuickSort
+ * on -Z (sim/heap.go:229-268), and the painted NRGBA canvas. */
+void orc_draw_order(int64_t n, const int64_t *z, int64_t *order);
+void orc_render(int64_t n, const double *x, const double *y, const double *rho, double mass,
+                const int64_t *order, int W, int H, uint8_t *rgba);
 
 #ifdef __cplusplus
 }

@@ -59,6 +59,14 @@ struct sph_handle {
     cudaStream_t stream = nullptr;
     int nsims = 0, k = 32, mode = MODE_EXACT64;
     int64_t n = 0;
+    int64_t cap_n = 0;   // particles the per-particle arrays hold (>= n; grows on sph_append)
+    int64_t n_eval = 0;  // particles whose density comes from the last force evaluation
+    // frames: draw keys per caller index (empty: caller order), ranks and buffers
+    std::vector<int64_t> zkeys;
+    bool zrank_dirty = true;
+    int32_t *d_zrank = nullptr, *d_rslot = nullptr, *d_fb = nullptr;
+    uchar4 *d_rgba = nullptr;
+    int64_t rank_cap = 0, fb_cap = 0;
     std::vector<sph_params> params;
     std::vector<int64_t> offs;
     std::vector<SimDev> hsims;
@@ -100,6 +108,13 @@ struct sph_handle {
     Launch launch() const { return Launch{sms, stream}; }
 };
 
+namespace sphgpu {
+void para_ramp_table(unsigned char out[256 * 4]);
+int set_ramp(const unsigned char rgba[256 * 4]);
+void launch_render(const Ctx &c, const Launch &L, const PArrays &A, const int32_t *zrank, int32_t *rslot,
+                   int32_t *fb, const double *rho, int64_t n_eval, double mass, int W, int H, uchar4 *out);
+}  // namespace sphgpu
+
 namespace {
 
 template <typename T>
@@ -116,8 +131,17 @@ int dalloc(sph_handle *h, T **p, size_t count) {
     return SPH_OK;
 }
 
-int alloc_parrays(sph_handle *h, PArrays &P, bool mixed) {
-    int64_t n = h->n;
+void dfree(sph_handle *h, void *p) {
+    if (!p) return;
+    for (size_t i = 0; i < h->allocs.size(); i++)
+        if (h->allocs[i] == p) {
+            h->allocs.erase(h->allocs.begin() + (long)i);
+            break;
+        }
+    cudaFree(p);
+}
+
+int alloc_parrays(sph_handle *h, PArrays &P, bool mixed, int64_t n) {
     int rc = 0;
     rc |= dalloc(h, &P.pos, n);
     rc |= dalloc(h, &P.vel, n);
@@ -131,6 +155,42 @@ int alloc_parrays(sph_handle *h, PArrays &P, bool mixed) {
     rc |= dalloc(h, &P.rec, n);
     if (mixed) rc |= dalloc(h, &P.vrec, n);
     return rc ? SPH_ERR_NOMEM : SPH_OK;
+}
+
+// Every per-particle array (state, evaluation copy, derived values, binning
+// keys, staging) for `cap` particles.
+int alloc_particles(sph_handle *h, int64_t cap) {
+    const bool mixed = h->mode == MODE_MIXED;
+    const int64_t k = h->k;
+    int rc = alloc_parrays(h, h->A, mixed, cap) | alloc_parrays(h, h->B, mixed, cap);
+    rc |= dalloc(h, &h->D.rho, cap);
+    rc |= dalloc(h, &h->D.c, cap);
+    rc |= dalloc(h, &h->D.h, cap);
+    rc |= dalloc(h, &h->D.nbr, cap * k);
+    rc |= dalloc(h, &h->D.defer, cap);
+    if (mixed) {
+        rc |= dalloc(h, &h->D.derf, cap);
+        rc |= dalloc(h, &h->D.d2f, cap * k);
+    } else {
+        rc |= dalloc(h, &h->D.der, cap);
+        rc |= dalloc(h, &h->D.dist, cap * k);
+    }
+    rc |= dalloc(h, &h->T.key, cap);
+    rc |= dalloc(h, &h->T.rank, cap);
+    rc |= dalloc(h, &h->T.tmp, cap);
+    h->io_doubles = (size_t)std::max<int64_t>(8 * cap, 3 * cap + 512);
+    rc |= dalloc(h, &h->d_io, h->io_doubles);
+    h->cap_n = cap;
+    return rc ? SPH_ERR_NOMEM : SPH_OK;
+}
+
+// Draw keys of appended particles (sph_append): kept only once keys exist.
+void draw_keys_append(sph_handle *h, int64_t n0, int64_t count, const int64_t *z) {
+    if (!z && h->zkeys.empty()) return;
+    if (h->zkeys.empty())
+        for (int64_t i = 0; i < n0; i++) h->zkeys.push_back(-i);  // caller order
+    for (int64_t i = 0; i < count; i++) h->zkeys.push_back(z ? z[i] : -(n0 + i));
+    h->zrank_dirty = true;
 }
 
 int check_params(const sph_params &p, int64_t n) {
@@ -354,27 +414,12 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     if (nsims > 1) rc |= dalloc(h, &h->d_simidx, total);
     rc |= dalloc(h, &h->d_flags, 1);
     if (rc) return bail(SPH_ERR_NOMEM);
-    if (alloc_parrays(h, h->A, mixed) || alloc_parrays(h, h->B, mixed)) return bail(SPH_ERR_NOMEM);
-    rc |= dalloc(h, &h->D.rho, n);
-    rc |= dalloc(h, &h->D.c, n);
-    rc |= dalloc(h, &h->D.h, n);
-    rc |= dalloc(h, &h->D.nbr, n * k);
-    if (mixed) {
-        rc |= dalloc(h, &h->D.derf, n);
-        rc |= dalloc(h, &h->D.d2f, n * k);
-    } else {
-        rc |= dalloc(h, &h->D.der, n);
-        rc |= dalloc(h, &h->D.dist, n * k);
-    }
+    if (alloc_particles(h, n)) return bail(SPH_ERR_NOMEM);
+    rc |= dalloc(h, &h->D.ndefer, 1);
     h->T.ncells = cells;
-    rc |= dalloc(h, &h->T.key, n);
-    rc |= dalloc(h, &h->T.rank, n);
-    rc |= dalloc(h, &h->T.tmp, n);
     rc |= dalloc(h, &h->T.count, cap);
     rc |= dalloc(h, &h->T.start, cap + 1);
     rc |= dalloc(h, &h->T.partial, cap / 4096 + 2);
-    h->io_doubles = (size_t)std::max<int64_t>(8 * n, 3 * n + 512);
-    rc |= dalloc(h, &h->d_io, h->io_doubles);
     if (rc) return bail(SPH_ERR_NOMEM);
     if (cudaMemset(h->T.count, 0, cap * sizeof(int32_t)) != cudaSuccess ||
         cudaMemset(h->D.nbr, 0, n * k * sizeof(int32_t)) != cudaSuccess ||
@@ -398,6 +443,8 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     h->tune.theta = 0.5f;
     h->tune.hgrow = 1.04f;
     h->tune.blocks_per_sm = std::max(1, knn_occupancy_blocks(h->tune.block, h->tune.cap, h->mode));
+    h->tune.tile = 1;
+    h->tune.tile_blocks_per_sm = std::max(1, knn_tile_occupancy_blocks((int)k, h->mode));
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(SPH_ERR_CUDA, cudaGetErrorString(e)));
     *out = h;
@@ -463,7 +510,7 @@ std::string tune_cache_path() {
 
 struct TuneChoice {
     float theta = 0.5f, hgrow = 1.04f;
-    int delta = 0;
+    int delta = 0, tile = 1;
     double ms = 0.0;
 };
 
@@ -480,7 +527,7 @@ bool tune_cache_get(const std::string &key, TuneChoice *c) {
     std::string line;
     bool found = false;
     while (std::getline(f, line)) {
-        if (line.rfind("sphgpu-tune-v1 " + key + " ", 0) != 0) continue;
+        if (line.rfind("sphgpu-tune-v2 " + key + " ", 0) != 0) continue;
         std::istringstream in(line.substr(16 + key.size()));
         std::string tok;
         while (in >> tok) {
@@ -490,6 +537,7 @@ bool tune_cache_get(const std::string &key, TuneChoice *c) {
             if (k == "theta") c->theta = std::stof(v);
             else if (k == "hgrow") c->hgrow = std::stof(v);
             else if (k == "delta") c->delta = std::stoi(v);
+            else if (k == "tile") c->tile = std::stoi(v);
             else if (k == "ms") c->ms = std::stod(v);
         }
         found = true;  // the last matching line wins
@@ -503,8 +551,8 @@ void tune_cache_put(const std::string &key, const TuneChoice &c) {
     std::filesystem::create_directories(std::filesystem::path(path).parent_path(), ec);
     std::ofstream f(path, std::ios::app);
     if (!f) return;
-    f << "sphgpu-tune-v1 " << key << " theta=" << c.theta << " hgrow=" << c.hgrow << " delta=" << c.delta
-      << " ms=" << c.ms << "\n";
+    f << "sphgpu-tune-v2 " << key << " theta=" << c.theta << " hgrow=" << c.hgrow << " delta=" << c.delta
+      << " tile=" << c.tile << " ms=" << c.ms << "\n";
 }
 
 }  // namespace
@@ -589,6 +637,76 @@ int sph_upload(sph_handle *h, const double *x, const double *y, const double *vx
     h->step = 0;
     h->uploaded = true;
     h->evaluated = false;
+    return SPH_OK;
+}
+
+int sph_append(sph_handle *h, int64_t count, const double *x, const double *y, const double *vx,
+               const double *vy, const double *u, const int64_t *z) {
+    if (!h || count < 0 || (count > 0 && (!x || !y))) return fail(SPH_ERR_ARG, "bad handle, count or arrays");
+    Guard g(h);
+    if (h->nsims != 1) return fail(SPH_ERR_ARG, "particles can be appended to a single simulation only");
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_append before sph_upload");
+    if (count == 0) return SPH_OK;
+    const int64_t n0 = h->n, n1 = n0 + count;
+    if (n1 >= kMaxParticles) return fail(SPH_ERR_ARG, "too many particles (limit 2^27)");
+    if (n1 > h->cap_n) {
+        // grow like a Go slice; only the state needs copying (the rest is rebuilt per evaluation)
+        const int64_t cap = std::min<int64_t>(std::max<int64_t>(n1, h->cap_n + h->cap_n / 2), kMaxParticles);
+        const PArrays oldA = h->A, oldB = h->B;
+        const Derived oldD = h->D;
+        const Tables oldT = h->T;
+        double *old_io = h->d_io;
+        if (alloc_particles(h, cap)) return fail(SPH_ERR_NOMEM, "cannot grow the particle arrays");
+        h->D.ndefer = oldD.ndefer;
+        h->T.count = oldT.count;
+        h->T.start = oldT.start;
+        h->T.partial = oldT.partial;
+        h->T.ncells = oldT.ncells;
+        auto cp = [&](void *dst, const void *src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        };
+        CUDA_TRY(cp(h->A.pos, oldA.pos, n0 * sizeof(double2)));
+        CUDA_TRY(cp(h->A.vel, oldA.vel, n0 * sizeof(double2)));
+        CUDA_TRY(cp(h->A.vp, oldA.vp, n0 * sizeof(double2)));
+        CUDA_TRY(cp(h->A.acc, oldA.acc, n0 * sizeof(double2)));
+        CUDA_TRY(cp(h->A.u, oldA.u, n0 * sizeof(double)));
+        CUDA_TRY(cp(h->A.up, oldA.up, n0 * sizeof(double)));
+        CUDA_TRY(cp(h->A.udot, oldA.udot, n0 * sizeof(double)));
+        CUDA_TRY(cp(h->A.id, oldA.id, n0 * sizeof(int32_t)));
+        CUDA_TRY(cp(h->A.hprev, oldA.hprev, n0 * sizeof(float)));
+        CUDA_TRY(cp(h->D.rho, oldD.rho, n0 * sizeof(double)));  // densities of the last evaluation (frames)
+        CUDA_TRY(cudaMemsetAsync(h->D.nbr, 0, (size_t)cap * h->k * sizeof(int32_t), h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        for (const PArrays *P : {&oldA, &oldB})
+            for (void *q : {(void *)P->pos, (void *)P->vel, (void *)P->vp, (void *)P->acc, (void *)P->u,
+                            (void *)P->up, (void *)P->udot, (void *)P->id, (void *)P->hprev, (void *)P->rec,
+                            (void *)P->vrec})
+                dfree(h, q);
+        for (void *q : {(void *)oldD.rho, (void *)oldD.c, (void *)oldD.h, (void *)oldD.nbr, (void *)oldD.defer,
+                        (void *)oldD.der, (void *)oldD.derf, (void *)oldD.dist, (void *)oldD.d2f,
+                        (void *)oldT.key, (void *)oldT.rank, (void *)oldT.tmp, (void *)old_io})
+            dfree(h, q);
+        if (h->d_nbr_io) {
+            cudaFree(h->d_nbr_io);
+            h->d_nbr_io = nullptr;
+        }
+    }
+    double *d = h->d_io;
+    const double *src[5] = {x, y, vx, vy, u};
+    for (int a = 0; a < 5; a++) {
+        if (src[a]) CUDA_TRY(cudaMemcpyAsync(d + a * count, src[a], count * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        else CUDA_TRY(cudaMemsetAsync(d + a * count, 0, count * sizeof(double), h->stream));
+    }
+    launch_append(h->launch(), h->A, n0, count, d);
+    CUDA_TRY(cudaGetLastError());
+    h->n = n1;
+    h->offs[1] = n1;
+    h->hsims[0].n = n1;
+    CUDA_TRY(cudaMemcpyAsync(h->d_sims, h->hsims.data(), sizeof(SimDev), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->d_offs, h->offs.data(), 2 * sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    draw_keys_append(h, n0, count, z);
+    destroy_graphs(h);
     return SPH_OK;
 }
 
@@ -678,7 +796,10 @@ int sph_step(sph_handle *h, int32_t nsteps) {
         CUDA_TRY(cudaGraphLaunch(h->g_step, h->stream));
         h->step++;
     }
-    if (nsteps > 0) h->evaluated = true;
+    if (nsteps > 0) {
+        h->evaluated = true;
+        h->n_eval = h->n;
+    }
     return check_flags(h);
 }
 
@@ -690,6 +811,7 @@ int sph_forces(sph_handle *h) {
     if (rc) return rc;
     CUDA_TRY(cudaGraphLaunch(h->g_forces, h->stream));
     h->evaluated = true;
+    h->n_eval = h->n;
     return check_flags(h);
 }
 
@@ -731,7 +853,10 @@ int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms) {
     float t = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&t, h->ev[0], h->ev[SPH_NUM_STAGES]));
     *ms = t;
-    if (nsteps > 0) h->evaluated = true;
+    if (nsteps > 0) {
+        h->evaluated = true;
+        h->n_eval = h->n;
+    }
     return check_flags(h);
 }
 
@@ -757,6 +882,7 @@ int sph_step_profiled(sph_handle *h, int32_t nsteps, double stage_ms[SPH_NUM_STA
         }
     }
     h->evaluated = true;
+    h->n_eval = h->n;
     return check_flags(h);
 }
 
@@ -765,6 +891,87 @@ int32_t sph_kernels_per_step(sph_handle *h) {
     Guard g(h);
     if (!h->g_step && ensure_graphs(h)) return -1;
     return h->kernels_per_step;
+}
+
+int sph_set_draw_keys(sph_handle *h, const int64_t *z) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (z) h->zkeys.assign(z, z + h->n);
+    else h->zkeys.clear();
+    h->zrank_dirty = true;
+    return SPH_OK;
+}
+
+int sph_render(sph_handle *h, int32_t width, int32_t height, uint8_t *rgba) {
+    if (!h || !rgba || width < 1 || height < 1 || width > 16384 || height > 16384)
+        return fail(SPH_ERR_ARG, "bad handle, buffer or frame size (1..16384 pixels per side)");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_render before sph_upload");
+    if (h->nsims != 1) return fail(SPH_ERR_ARG, "frames are drawn for a single simulation");
+    const int64_t npix = (int64_t)width * height;
+    if (h->rank_cap < h->cap_n) {
+        dfree(h, h->d_zrank);
+        dfree(h, h->d_rslot);
+        h->d_zrank = h->d_rslot = nullptr;
+        if (dalloc(h, &h->d_zrank, h->cap_n) || dalloc(h, &h->d_rslot, h->cap_n))
+            return fail(SPH_ERR_NOMEM, "frame buffers");
+        h->rank_cap = h->cap_n;
+        h->zrank_dirty = true;
+        unsigned char lut[256 * 4];
+        para_ramp_table(lut);
+        if (set_ramp(lut)) return fail(SPH_ERR_CUDA, "colour table upload failed");
+    }
+    if (h->fb_cap < npix) {
+        dfree(h, h->d_fb);
+        dfree(h, h->d_rgba);
+        h->d_fb = nullptr;
+        h->d_rgba = nullptr;
+        if (dalloc(h, &h->d_fb, npix) || dalloc(h, &h->d_rgba, npix)) return fail(SPH_ERR_NOMEM, "frame buffers");
+        h->fb_cap = npix;
+    }
+    const int64_t n = h->n;
+    if (!h->zkeys.empty() && (int64_t)h->zkeys.size() != n)
+        return fail(SPH_ERR_STATE, "draw keys do not match the particle count");
+    if (!h->zkeys.empty() && h->zrank_dirty) {
+        // painting order: descending Z (the reference sorts by -Z), ties by caller index
+        std::vector<int32_t> order((size_t)n), rank((size_t)n);
+        for (int64_t i = 0; i < n; i++) order[(size_t)i] = (int32_t)i;
+        const std::vector<int64_t> &z = h->zkeys;
+        std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return z[a] > z[b] || (z[a] == z[b] && a < b); });
+        for (int64_t r = 0; r < n; r++) rank[(size_t)order[(size_t)r]] = (int32_t)r;
+        CUDA_TRY(cudaMemcpyAsync(h->d_zrank, rank.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        h->zrank_dirty = false;
+    }
+    launch_render(h->ctx(), h->launch(), h->A, h->zkeys.empty() ? nullptr : h->d_zrank, h->d_rslot, h->d_fb,
+                  h->D.rho, h->evaluated ? h->n_eval : 0, h->params[0].mass, width, height, h->d_rgba);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(rgba, h->d_rgba, npix * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_set_search(sph_handle *h, int32_t tiles) {
+    if (!h || (tiles != 0 && tiles != 1)) return fail(SPH_ERR_ARG, "bad handle or search path");
+    Guard g(h);
+    if (h->tune.tile != tiles) {
+        h->tune.tile = tiles;
+        destroy_graphs(h);
+    }
+    return SPH_OK;
+}
+
+int sph_search_stats(sph_handle *h, int64_t *queries, int64_t *deferred) {
+    if (!h || !queries || !deferred) return fail(SPH_ERR_ARG, "bad argument");
+    Guard g(h);
+    int32_t nd = 0;
+    if (h->tune.tile && h->evaluated) {
+        CUDA_TRY(cudaMemcpyAsync(&nd, h->D.ndefer, sizeof nd, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    *queries = h->n;
+    *deferred = h->tune.tile ? nd : h->n;
+    return SPH_OK;
 }
 
 int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches) {
@@ -815,24 +1022,35 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
     int trials = 0;
     const int reps = std::max(1, std::min(3, (int)(150.0 / std::max(ms0, 1e-3))));
     if (!cached) {
-        const float thetas[] = {0.35f, 0.5f, 0.7f, 1.0f};
+        // (search path, cell side / radius): group tiles (theta then only shapes
+        // the deferred queries' search) or the per-query search
+        const int tiles[] = {1, 0, 0, 0};
+        const float thetas[] = {0.5f, 0.35f, 0.5f, 0.7f};
         const float hgrows[] = {1.02f, 1.04f, 1.08f};
         best.ms = 1e300;
         const int dmax = (cv < 0.6) ? 1 : 2;  // clustered data: dense regions want finer cells
         for (int delta = -1; delta <= dmax; delta++) {
             if ((rc = apply_levels(h, delta))) continue;
-            for (float th : thetas) {
-                h->tune.theta = th;
+            for (int v = 0; v < 4; v++) {
+                h->tune.tile = tiles[v];
+                h->tune.theta = thetas[v];
                 h->tune.hgrow = 1.04f;
                 destroy_graphs(h);
                 double ms = 0.0;
                 if ((rc = time_forces(h, reps, &ms))) return rc;
                 trials++;
-                if (ms < best.ms) { best.ms = ms; best.theta = th; best.delta = delta; best.hgrow = 1.04f; }
+                if (ms < best.ms) {
+                    best.ms = ms;
+                    best.theta = thetas[v];
+                    best.tile = tiles[v];
+                    best.delta = delta;
+                    best.hgrow = 1.04f;
+                }
             }
         }
         if ((rc = apply_levels(h, best.delta))) return rc;
         h->tune.theta = best.theta;
+        h->tune.tile = best.tile;
         for (float hg : hgrows) {
             if (hg == 1.04f) continue;
             h->tune.hgrow = hg;
@@ -847,6 +1065,7 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
     h->tune = base;
     h->tune.theta = best.theta;
     h->tune.hgrow = best.hgrow;
+    h->tune.tile = best.tile;
     if ((rc = apply_levels(h, best.delta))) return rc;
     // back to the uploaded state
     launch_scatter_state(h->ctx(), h->launch(), h->A, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, nullptr, nullptr,
@@ -858,6 +1077,7 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
         std::ostringstream o;
         o << "{\"key\": \"" << key << "\", \"cached\": " << (cached ? "true" : "false") << ", \"trials\": " << trials
           << ", \"theta\": " << best.theta << ", \"hgrow\": " << best.hgrow << ", \"level_delta\": " << best.delta
+          << ", \"tiles\": " << best.tile
           << ", \"ms_per_eval\": " << best.ms << ", \"ms_default\": " << ms0 << ", \"h_cv\": " << cv
           << ", \"cache\": \"" << tune_cache_path() << "\"}";
         strncpy(report, o.str().c_str(), (size_t)report_len - 1);
@@ -870,12 +1090,13 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
 namespace {
 struct CkptHeader {
     char magic[8];      // "SPHGPUCK"
-    uint32_t version;   // 1
+    uint32_t version;   // 2
     uint32_t mode;
     int64_t n;
     int32_t nsims, k, step, level_delta;
     uint64_t params_hash;
     float theta, hgrow;  // search shape (the mixed form's sums follow its visiting order)
+    int32_t tile, pad;   // search path (group tiles or per query)
 };
 
 uint64_t fnv1a(const void *p, size_t len, uint64_t hsh = 1469598103934665603ull) {
@@ -909,7 +1130,7 @@ int sph_save(sph_handle *h, const char *path) {
     CkptHeader hd;
     memset(&hd, 0, sizeof hd);
     memcpy(hd.magic, "SPHGPUCK", 8);
-    hd.version = 1;
+    hd.version = 2;
     hd.mode = (uint32_t)h->mode;
     hd.n = h->n;
     hd.nsims = h->nsims;
@@ -919,6 +1140,7 @@ int sph_save(sph_handle *h, const char *path) {
     hd.params_hash = params_hash(h);
     hd.theta = h->tune.theta;
     hd.hgrow = h->tune.hgrow;
+    hd.tile = h->tune.tile;
     std::ofstream f(path, std::ios::binary | std::ios::trunc);
     if (!f) return fail(SPH_ERR_ARG, std::string("cannot write ") + path);
     f.write((const char *)&hd, sizeof hd);
@@ -940,16 +1162,17 @@ int sph_load(sph_handle *h, const char *path) {
     if (!f) return fail(SPH_ERR_ARG, std::string("cannot read ") + path);
     CkptHeader hd;
     f.read((char *)&hd, sizeof hd);
-    if (!f || memcmp(hd.magic, "SPHGPUCK", 8) != 0 || hd.version != 1)
-        return fail(SPH_ERR_ARG, "not a version-1 SPH checkpoint");
+    if (!f || memcmp(hd.magic, "SPHGPUCK", 8) != 0 || hd.version != 2)
+        return fail(SPH_ERR_ARG, "not a version-2 SPH checkpoint");
     if (hd.n != h->n || hd.nsims != h->nsims || hd.k != h->k || hd.mode != (uint32_t)h->mode ||
         hd.params_hash != params_hash(h))
         return fail(SPH_ERR_ARG, "checkpoint was written by a handle with other parameters or sizes");
     int rc;
     if (hd.level_delta != h->level_delta && (rc = apply_levels(h, hd.level_delta))) return rc;
-    if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow) {
+    if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow || hd.tile != h->tune.tile) {
         h->tune.theta = hd.theta;
         h->tune.hgrow = hd.hgrow;
+        h->tune.tile = hd.tile;
         destroy_graphs(h);
     }
     std::vector<char> buf;

@@ -82,6 +82,8 @@ struct Derived {
     double2 *dist;  // FP64 modes: n*k squared distance from the search, then
                     // (NNDists, NNDists/h) [bit-exact form] or (NNDists, 1/NNDists) [fast form]
     float *d2f;     // mixed: n*k FP32 squared distances
+    int32_t *defer;  // queries the group-tile search leaves to the per-query search (n)
+    int32_t *ndefer; // their count
 };
 
 struct Tables {
@@ -215,6 +217,8 @@ struct KnnTune {
     float theta;    // cell side >= theta * search radius
     float hgrow;    // radius guess = hgrow * previous h
     int blocks_per_sm; // resident blocks per SM at this block size / capacity
+    int tile;          // 1: group tiles first, per-query search for the deferred queries
+    int tile_blocks_per_sm;
 };
 void knn_init_attrs();
 void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D,
@@ -228,6 +232,7 @@ void launch_gather_state(const Ctx &c, const Launch &L, const PArrays &A, double
 void launch_scatter_state(const Ctx &c, const Launch &L, const PArrays &A, const double *x,
                           const double *y, const double *vx, const double *vy, const double *u,
                           const double *ax, const double *ay, const double *udot, bool have_acc);
+void launch_append(const Launch &L, const PArrays &A, int64_t n0, int64_t count, const double *buf);
 void launch_gather_derived(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D,
                            double *rho, double *cs, double *h);
 void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &A, const PArrays &B,
@@ -235,6 +240,7 @@ void launch_gather_neighbours(const Ctx &c, const Launch &L, const PArrays &A, c
 void launch_diagnostics(const Ctx &c, const Launch &L, const PArrays &A, const Derived &D,
                         int64_t lo, int64_t hi, double *scratch);
 int knn_occupancy_blocks(int block, int cap, int mode);
+int knn_tile_occupancy_blocks(int k, int mode);
 int probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost);
 int div_selftest(int64_t n, uint64_t seed, long long *mismatches);
 // message returned by sph_last_error() on this thread

@@ -498,12 +498,13 @@ int64_t sph_config_start_count(const sph_config *cfg) {
     return n;
 }
 
-int sph_config_spawn(const sph_config *cfg, double *x, double *y, double *vx, double *vy, double *u) {
+int sph_config_spawn(const sph_config *cfg, double *x, double *y, double *vx, double *vy, double *u, int64_t *z) {
     if (!cfg || !x || !y) return SPH_ERR_ARG;
     int64_t o = 0;
     for (int s = 0; s < cfg->nstart; s++) {
         const sph_rect_spawner &sp = cfg->start[s];
         SplitMix64 r(12345678);  // reseeded per spawner, as sim/config-parser.go:63
+        const int64_t o0 = o;
         for (int64_t i = 0; i < sp.n; i++, o++) {
             x[o] = sp.upper_left[0] + r.uni() * (sp.lower_right[0] - sp.upper_left[0]);
             y[o] = sp.upper_left[1] + r.uni() * (sp.lower_right[1] - sp.upper_left[1]);
@@ -511,12 +512,17 @@ int sph_config_spawn(const sph_config *cfg, double *x, double *y, double *vx, do
             if (vy) vy[o] = 0.0;
             if (u) u[o] = 0.01;
         }
+        // then Z = rand.Int() per particle (a second pass, as sim/config-parser.go:73-76)
+        for (int64_t i = 0; i < sp.n; i++) {
+            const int64_t zi = (int64_t)(r.next() >> 1);
+            if (z) z[o0 + i] = zi;
+        }
     }
     return SPH_OK;
 }
 
 int64_t sph_point_source_spawn(sph_point_source *src, double t, uint64_t seed, double *x, double *y, double *vx,
-                               double *vy, double *u) {
+                               double *vy, double *u, int64_t *z) {
     if (!src || !(src->rate > 0)) return 0;
     const double dt = t - src->last_spawned;
     const double cooldown = 1.0 / src->rate;
@@ -528,14 +534,35 @@ int64_t sph_point_source_spawn(sph_point_source *src, double t, uint64_t seed, d
         for (int64_t i = 0; i < n; i++) {
             const double dy = 0.01 * (-1.0 + 2.0 * r.uni());
             const double dx = 0.01 * (-1.0 + 2.0 * r.uni());
+            const int64_t zi = (int64_t)(r.next() >> 1);  // Z = rand.Int()
             x[i] = src->origin[0] + dx;
             y[i] = src->origin[1] + dy;
             if (vx) vx[i] = 0.0;
             if (vy) vy[i] = 0.0;
             if (u) u[i] = 0.002;
+            if (z) z[i] = zi;
         }
     }
     return n;
 }
 
 }  // extern "C"
+
+namespace sphgpu {
+
+// gx.ParaRamp (gx/graphics.go:156-164) for every index, in FP64 without
+// contraction (this file is compiled with -ffp-contract=off), as NRGBA bytes.
+void para_ramp_table(unsigned char out[256 * 4]) {
+    for (int i = 0; i < 256; i++) {
+        const double x = (double)i;
+        const double r = std::fmin(215.0, std::fmax(0.0, -std::fabs((x - 60) * 31 / 17 - 232) + 245));
+        const double g = std::fmin(190.0, std::fmax(0.0, -std::fabs(x * 31 / 17 - 232) + 245));
+        const double b = std::fmin(215.0, std::fmax(0.0, -std::fabs((x + 70) * 31 / 17 - 232) + 245));
+        out[4 * i + 0] = (unsigned char)r;
+        out[4 * i + 1] = (unsigned char)g;
+        out[4 * i + 2] = (unsigned char)b;
+        out[4 * i + 3] = 255;
+    }
+}
+
+}  // namespace sphgpu

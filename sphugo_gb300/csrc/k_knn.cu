@@ -38,6 +38,7 @@ struct KnnArgs {
     Derived D;
     const int32_t *start;
     float theta, hgrow;
+    int use_defer;  // per-query kernel: walk the deferred list instead of every particle
 };
 
 // |d2_f32 - d2_ref| <= kEpsRel * d2 + eps_abs(R): the float-pair difference
@@ -103,6 +104,188 @@ __device__ __forceinline__ bool exact_greater(const PArrays &B, unsigned long lo
     return (ca & 15u) > (cb & 15u);
 }
 
+// Exact selection of the k nearest among the m entries of a warp's list
+// (skey: FP32 squared distances as bits, scode: (j << kCodeShift) | image)
+// for query q, written to the neighbour list (slot 0 nearest in the FP64
+// forms; the mixed form writes the set with the farthest in the last slot).
+// Returns 0 when written, or 1 when the k-th FP32 value lies too close to the
+// search radius R for the list to be complete (*Rnext: a radius that is).
+template <int MODE, int NR>
+__device__ int select_write(const KnnArgs &a, const SimDev &S, int64_t q, int m, float R, float epsabs,
+                            uint32_t *skey, uint32_t *scode, uint32_t *sord, unsigned long long *sexact,
+                            int lane, float *Rnext) {
+    using LS = ListShape<NR>;
+    const int k = a.c.k;
+    const PArrays &B = a.B;
+    const float R2 = R * R;
+    uint32_t v[NR];
+    float tau, eps;
+    if (MODE == MODE_MIXED) {
+        // The mixed form needs the set, not the order: drop the m-k largest
+        // (unique keys: truncated FP32 value | slot) by warp max-reductions,
+        // then verify with the full FP32 values that every kept entry lies
+        // more than 2 eps below every dropped one and that the farthest kept
+        // entry is unique by 2 eps.
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int e = (r << 5) | lane;
+            // bit 31 tags a live entry (FP32 squared distances are >= 0)
+            v[r] = e < m ? (0x80000000u | (skey[e] & ~LS::SMASK) | (uint32_t)e) : 0u;
+        }
+        uint32_t dropped_min = 0xffffffffu;  // smallest full FP32 bits among dropped entries
+        for (int it = 0; it < m - k; it++) {
+            uint32_t lm = 0;
+#pragma unroll
+            for (int r = 0; r < NR; r++) lm = max(lm, v[r]);
+            const uint32_t gm = __reduce_max_sync(0xffffffffu, lm);
+#pragma unroll
+            for (int r = 0; r < NR; r++)
+                if (v[r] == gm) v[r] = 0u;
+            dropped_min = min(dropped_min, skey[gm & LS::SMASK]);
+        }
+        // largest and second largest full values among the kept entries
+        uint32_t top = 0, second = 0;  // tagged with bit 31 when set
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            if (v[r]) {
+                const uint32_t f = 0x80000000u | skey[v[r] & LS::SMASK];
+                if (f > top) { second = top; top = f; } else if (f > second) second = f;
+            }
+        }
+        const uint32_t gtop = __reduce_max_sync(0xffffffffu, top);
+        // second: the largest of (each lane's top unless it is the global top) and seconds
+        const uint32_t cand2 = top == gtop ? second : top;
+        const uint32_t g2 = __reduce_max_sync(0xffffffffu, cand2);
+        const uint32_t nties = __popc(__ballot_sync(0xffffffffu, top == gtop));
+        tau = __uint_as_float(gtop & 0x7fffffffu);
+        eps = eps_of(tau, epsabs * R);
+        if (tau + 3.f * eps > R2 * (1.f - 4.8e-7f)) {
+            *Rnext = sqrtf((tau + 3.f * eps) * 1.00002f) * 1.0001f;
+            return 1;
+        }
+        const float fd = __uint_as_float(dropped_min), f2 = __uint_as_float(g2 & 0x7fffffffu);
+        const bool set_ok = (m == k) || (fd - tau > 2.f * eps_of(fd, epsabs * R));
+        const bool top_ok = nties == 1 && (k == 1 || tau - f2 > 2.f * eps);
+        if (set_ok && top_ok) {
+            // write the kept entries in slot order, the farthest last
+            int pos = 0;
+#pragma unroll
+            for (int r = 0; r < NR; r++) {
+                const bool live = v[r] != 0u;
+                const bool is_top = live && (0x80000000u | skey[v[r] & LS::SMASK]) == gtop;
+                const bool keep = live && !is_top;
+                const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int o = pos + __popc(bal & lanemask_lt());
+                    const uint32_t sl = v[r] & LS::SMASK;
+                    a.D.nbr[q * k + o] = (int32_t)scode[sl];
+                    a.D.d2f[q * k + o] = __uint_as_float(skey[sl]);
+                }
+                if (is_top) {
+                    const uint32_t sl = v[r] & LS::SMASK;
+                    a.D.nbr[q * k + k - 1] = (int32_t)scode[sl];
+                    a.D.d2f[q * k + k - 1] = __uint_as_float(skey[sl]);
+                }
+                pos += __popc(bal);
+            }
+            __syncwarp();
+            return 0;
+        }
+        // otherwise the sorted path below decides
+    }
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+        const int e = (r << 5) | lane;
+        v[r] = e < m ? ((skey[e] & ~LS::SMASK) | (uint32_t)e) : 0xffffffffu;
+    }
+    bitonic_sort<NR>(v, lane);
+#pragma unroll
+    for (int r = 0; r < NR; r++) sord[(r << 5) | lane] = v[r] & LS::SMASK;
+    __syncwarp();
+    // tau: the largest FP32 value among the first k in truncated order (>= the k-th smallest)
+    float tmax = 0.f;
+    for (int e = lane; e < k; e += 32) tmax = fmaxf(tmax, __uint_as_float(skey[sord[e]]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+    tau = tmax;
+    eps = eps_of(tau, epsabs * R);
+    if (tau + 3.f * eps > R2 * (1.f - 4.8e-7f)) {
+        *Rnext = sqrtf((tau + 3.f * eps) * 1.00002f) * 1.0001f;
+        __syncwarp();
+        return 1;
+    }
+
+    // ---- S = every entry whose FP32 value is within 2 eps of tau (a prefix)
+    const float lim = tau + 2.f * eps;
+    int last = -1;
+    for (int e = lane; e < m; e += 32)
+        if (__uint_as_float(skey[sord[e]]) <= lim) last = e;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+    const int send = last + 1;  // >= k
+
+    // ---- orders the FP32 values cannot decide: FP64 keys, exact runs
+    bool unc = false;
+    for (int e = lane; e + 1 < send; e += 32) {
+        const float fa = __uint_as_float(skey[sord[e]]), fb = __uint_as_float(skey[sord[e + 1]]);
+        unc |= (fb - fa) <= 2.f * eps_of(fb, epsabs * R);
+    }
+    if (__any_sync(0xffffffffu, unc)) {
+        const double2 P = B.pos[q];
+        for (int e = lane; e < send; e += 32) {
+            const float fe = __uint_as_float(skey[sord[e]]);
+            bool need = false;
+            if (e + 1 < send) {
+                const float fn = __uint_as_float(skey[sord[e + 1]]);
+                need |= (fn - fe) <= 2.f * eps_of(fn, epsabs * R);
+            }
+            if (e > 0) need |= (fe - __uint_as_float(skey[sord[e - 1]])) <= 2.f * eps_of(fe, epsabs * R);
+            if (need) {
+                const uint32_t code = scode[sord[e]];
+                double ox, oy;
+                img_shift(S, code & 15u, ox, oy);
+                const double2 Q = B.pos[code >> kCodeShift];
+                sexact[e] = (unsigned long long)__double_as_longlong(dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y));
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            int rs = 0;
+            for (int e = 0; e < send; e++) {
+                bool brk = (e + 1 == send);
+                if (!brk) {
+                    const float fa = __uint_as_float(skey[sord[e]]), fb = __uint_as_float(skey[sord[e + 1]]);
+                    brk = (fb - fa) > 2.f * eps_of(fb, epsabs * R);
+                }
+                if (brk) {
+                    // insertion sort of the run [rs, e] by (exact d2, id, image)
+                    for (int x = rs + 1; x <= e; x++) {
+                        const unsigned long long kk = sexact[x];
+                        const uint32_t so = sord[x];
+                        int f = x - 1;
+                        while (f >= rs && exact_greater(B, sexact[f], scode[sord[f]], kk, scode[so])) {
+                            sexact[f + 1] = sexact[f];
+                            sord[f + 1] = sord[f];
+                            f--;
+                        }
+                        sexact[f + 1] = kk;
+                        sord[f + 1] = so;
+                    }
+                    rs = e + 1;
+                }
+            }
+        }
+        __syncwarp();
+    }
+    // ---- write the sorted list (slot 0 = nearest)
+    for (int e = lane; e < k; e += 32) {
+        a.D.nbr[q * k + e] = (int32_t)scode[sord[e]];
+        if (MODE == MODE_MIXED) a.D.d2f[q * k + e] = __uint_as_float(skey[sord[e]]);
+    }
+    __syncwarp();
+    return 0;
+}
+
 template <int MODE, int NR>
 __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
     using LS = ListShape<NR>;
@@ -119,7 +302,9 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
     const PArrays &B = a.B;
     unsigned fl = 0;
 
-    for (int64_t q = (int64_t)blockIdx.x * wpb + w; q < a.c.n; q += (int64_t)gridDim.x * wpb) {
+    const int64_t nq = a.use_defer ? (int64_t)*a.D.ndefer : a.c.n;
+    for (int64_t qi = (int64_t)blockIdx.x * wpb + w; qi < nq; qi += (int64_t)gridDim.x * wpb) {
+        const int64_t q = a.use_defer ? (int64_t)a.D.defer[qi] : qi;
         // Only FP32 / integer work below (FP64 would run 32-wide for one query).
         const int s = sim_of(a.c, q);
         const SimDev &S = a.c.sims[s];
@@ -156,9 +341,8 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
             }
         }
         const float Rmax = 2.5f * Lmax;
-        float Rlo = 0.f, Rhi = 3.0e38f, tau = 0.f, eps = 0.f;
+        float Rlo = 0.f, Rhi = 3.0e38f;
         int m = 0, ok = 0;
-        uint32_t v[NR];
         for (int att = 0; att < 48; att++) {
             __syncwarp();  // the previous attempt's reads of the list are done
             R = fminf(R, Rmax);
@@ -268,99 +452,10 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
                 continue;
             }
             __syncwarp();
-            if (MODE == MODE_MIXED) {
-                // The mixed form needs the set, not the order: drop the m-k
-                // largest (unique keys: truncated FP32 value | slot) by warp
-                // max-reductions, then verify with the full FP32 values that
-                // every kept entry lies more than 2 eps below every dropped one
-                // and that the farthest kept entry is unique by 2 eps.
-#pragma unroll
-                for (int r = 0; r < NR; r++) {
-                    const int e = (r << 5) | lane;
-                    // bit 31 tags a live entry (FP32 squared distances are >= 0)
-                    v[r] = e < m ? (0x80000000u | (skey[e] & ~LS::SMASK) | (uint32_t)e) : 0u;
-                }
-                uint32_t dropped_min = 0xffffffffu;  // smallest full FP32 bits among dropped entries
-                for (int it = 0; it < m - k; it++) {
-                    uint32_t lm = 0;
-#pragma unroll
-                    for (int r = 0; r < NR; r++) lm = max(lm, v[r]);
-                    const uint32_t gm = __reduce_max_sync(0xffffffffu, lm);
-#pragma unroll
-                    for (int r = 0; r < NR; r++)
-                        if (v[r] == gm) v[r] = 0u;
-                    dropped_min = min(dropped_min, skey[gm & LS::SMASK]);
-                }
-                // largest and second largest full values among the kept entries
-                uint32_t top = 0, second = 0;  // tagged with bit 31 when set
-#pragma unroll
-                for (int r = 0; r < NR; r++) {
-                    if (v[r]) {
-                        const uint32_t f = 0x80000000u | skey[v[r] & LS::SMASK];
-                        if (f > top) { second = top; top = f; } else if (f > second) second = f;
-                    }
-                }
-                const uint32_t gtop = __reduce_max_sync(0xffffffffu, top);
-                // second: the largest of (each lane's top unless it is the global top) and seconds
-                const uint32_t cand2 = top == gtop ? second : top;
-                const uint32_t g2 = __reduce_max_sync(0xffffffffu, cand2);
-                const uint32_t nties = __popc(__ballot_sync(0xffffffffu, top == gtop));
-                tau = __uint_as_float(gtop & 0x7fffffffu);
-                eps = eps_of(tau, epsabs * R);
-                if (tau + 3.f * eps > R2 * (1.f - 4.8e-7f)) {
-                    Rlo = R;
-                    R = sqrtf((tau + 3.f * eps) * 1.00002f) * 1.0001f;
-                    continue;
-                }
-                const float fd = __uint_as_float(dropped_min), f2 = __uint_as_float(g2 & 0x7fffffffu);
-                const bool set_ok = (m == k) || (fd - tau > 2.f * eps_of(fd, epsabs * R));
-                const bool top_ok = nties == 1 && (k == 1 || tau - f2 > 2.f * eps);
-                if (set_ok && top_ok) {
-                    // write the kept entries in slot order, the farthest last
-                    int pos = 0;
-#pragma unroll
-                    for (int r = 0; r < NR; r++) {
-                        const bool live = v[r] != 0u;
-                        const bool is_top = live && (0x80000000u | skey[v[r] & LS::SMASK]) == gtop;
-                        const bool keep = live && !is_top;
-                        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-                        if (keep) {
-                            const int o = pos + __popc(bal & lanemask_lt());
-                            const uint32_t sl = v[r] & LS::SMASK;
-                            a.D.nbr[q * k + o] = (int32_t)scode[sl];
-                            a.D.d2f[q * k + o] = __uint_as_float(skey[sl]);
-                        }
-                        if (is_top) {
-                            const uint32_t sl = v[r] & LS::SMASK;
-                            a.D.nbr[q * k + k - 1] = (int32_t)scode[sl];
-                            a.D.d2f[q * k + k - 1] = __uint_as_float(skey[sl]);
-                        }
-                        pos += __popc(bal);
-                    }
-                    ok = 2;  // written
-                    break;
-                }
-                // otherwise fall through to the sorted path below
-            }
-#pragma unroll
-            for (int r = 0; r < NR; r++) {
-                const int e = (r << 5) | lane;
-                v[r] = e < m ? ((skey[e] & ~LS::SMASK) | (uint32_t)e) : 0xffffffffu;
-            }
-            bitonic_sort<NR>(v, lane);
-#pragma unroll
-            for (int r = 0; r < NR; r++) sord[(r << 5) | lane] = v[r] & LS::SMASK;
-            __syncwarp();
-            // tau: the largest FP32 value among the first k in truncated order (>= the k-th smallest)
-            float tmax = 0.f;
-            for (int e = lane; e < k; e += 32) tmax = fmaxf(tmax, __uint_as_float(skey[sord[e]]));
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
-            tau = tmax;
-            eps = eps_of(tau, epsabs * R);
-            if (tau + 3.f * eps > R2 * (1.f - 4.8e-7f)) {
+            float Rn;
+            if (select_write<MODE, NR>(a, S, q, m, R, epsabs, skey, scode, sord, sexact, lane, &Rn)) {
                 Rlo = R;
-                R = sqrtf((tau + 3.f * eps) * 1.00002f) * 1.0001f;
+                R = Rn;
                 continue;
             }
             ok = 1;
@@ -372,83 +467,386 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
                 a.D.nbr[q * k + e] = ((int32_t)q << kCodeShift) | 4;
                 if (MODE == MODE_MIXED) a.D.d2f[q * k + e] = 0.f;
             }
-            continue;
-        }
-        if (ok == 2) {
-            __syncwarp();
-            continue;
-        }
-
-        // ---- S = every entry whose FP32 value is within 2 eps of tau (a prefix)
-        const float lim = tau + 2.f * eps;
-        int last = -1;
-        for (int e = lane; e < m; e += 32)
-            if (__uint_as_float(skey[sord[e]]) <= lim) last = e;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
-        const int send = last + 1;  // >= k
-
-        // ---- orders the FP32 values cannot decide: FP64 keys, exact runs
-        bool unc = false;
-        for (int e = lane; e + 1 < send; e += 32) {
-            const float fa = __uint_as_float(skey[sord[e]]), fb = __uint_as_float(skey[sord[e + 1]]);
-            unc |= (fb - fa) <= 2.f * eps_of(fb, epsabs * R);
-        }
-        if (__any_sync(0xffffffffu, unc)) {
-            const double2 P = B.pos[q];
-            for (int e = lane; e < send; e += 32) {
-                const float fe = __uint_as_float(skey[sord[e]]);
-                bool need = false;
-                if (e + 1 < send) {
-                    const float fn = __uint_as_float(skey[sord[e + 1]]);
-                    need |= (fn - fe) <= 2.f * eps_of(fn, epsabs * R);
-                }
-                if (e > 0) need |= (fe - __uint_as_float(skey[sord[e - 1]])) <= 2.f * eps_of(fe, epsabs * R);
-                if (need) {
-                    const uint32_t code = scode[sord[e]];
-                    double ox, oy;
-                    img_shift(S, code & 15u, ox, oy);
-                    const double2 Q = B.pos[code >> kCodeShift];
-                    sexact[e] = (unsigned long long)__double_as_longlong(dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y));
-                }
-            }
-            __syncwarp();
-            if (lane == 0) {
-                int rs = 0;
-                for (int e = 0; e < send; e++) {
-                    bool brk = (e + 1 == send);
-                    if (!brk) {
-                        const float fa = __uint_as_float(skey[sord[e]]), fb = __uint_as_float(skey[sord[e + 1]]);
-                        brk = (fb - fa) > 2.f * eps_of(fb, epsabs * R);
-                    }
-                    if (brk) {
-                        // insertion sort of the run [rs, e] by (exact d2, id, image)
-                        for (int x = rs + 1; x <= e; x++) {
-                            const unsigned long long kk = sexact[x];
-                            const uint32_t so = sord[x];
-                            int f = x - 1;
-                            while (f >= rs && exact_greater(B, sexact[f], scode[sord[f]], kk, scode[so])) {
-                                sexact[f + 1] = sexact[f];
-                                sord[f + 1] = sord[f];
-                                f--;
-                            }
-                            sexact[f + 1] = kk;
-                            sord[f + 1] = so;
-                        }
-                        rs = e + 1;
-                    }
-                }
-            }
-            __syncwarp();
-        }
-        // ---- write the sorted list (slot 0 = nearest)
-        for (int e = lane; e < k; e += 32) {
-            a.D.nbr[q * k + e] = (int32_t)scode[sord[e]];
-            if (MODE == MODE_MIXED) a.D.d2f[q * k + e] = __uint_as_float(skey[sord[e]]);
         }
         __syncwarp();
     }
     if (fl && lane == 0) atomicOr(a.c.flags, fl);
+}
+
+// ---------------------------------------------------------------- group tiles
+// k_knn_tile, one warp per group of 32 consecutive particles (consecutive in
+// the Morton-sorted order, hence spatially compact), one lane per query:
+//   1. every query takes the radius guess R = hgrow * previous h and the
+//      rectangle of finest cells covering its square of half side R + tol;
+//      the union of the rectangles is bounded by a box, taken at the finest
+//      level with <= kTileBox cells and <= kTileRows rows;
+//   2. each row of the box keeps the hull of the query rectangles crossing
+//      it; the cells of those row hulls are contiguous particle ranges of the
+//      sorted order, copied once into a shared-memory tile as FP32 positions
+//      relative to the group's first particle (image shift applied in FP64
+//      before the rounding) with their neighbour codes;
+//   3. each lane scans the whole tile for its own query (broadcast reads) and
+//      keeps every record within R as a 32-bit key: the squared distance in
+//      units of R^2 / 2^23 (23 bits) above the tile slot (9 bits);
+//   4. each lane keeps its k+1 smallest keys in ascending order (a
+//      branch-free insertion chain in registers; an insertion sort in its
+//      shared-memory column for k > 37) and accepts the first k when the FP32
+//      values decide them:
+//      the k-th lies 3 eps inside R (the tile held every candidate), the
+//      (k+1)-th lies more than 2 eps beyond it (the set), and in the FP64
+//      forms every neighbour is more than 2 eps from the next (the order;
+//      the mixed form needs only the farthest to be unique, it fixes h).
+// eps bounds |FP32 key - reference FP64 squared distance|: 2^-20 d2 for the
+// products, 2^-20 D R for the relative coordinates (|coordinate| <= D),
+// 2^-21 R^2 for the 23-bit key, and the reference's own rounding of p + offset.
+// Every other query goes to the deferred list that the per-query kernel
+// finishes: short or overflowing lists, undecided sets or orders, tiles over
+// capacity, no previous smoothing length (first evaluation), and queries of
+// a group's second simulation (ensembles). Both paths return the same exact
+// neighbour sets and, in the FP64 forms, the same order.
+constexpr int kTileWarps = 4;
+constexpr int kTileCap = 512;  // 9-bit tile slots
+constexpr int kTileRows = 64;
+constexpr int kTileBox = 1024;
+
+template <int NR>
+struct TileSmem {
+    static constexpr int LCAP = 24 * NR;  // per-query list capacity (>= 1.5 k)
+    // k <= 37: the k+1 smallest keys are kept in A registers per lane
+    static constexpr bool REG = NR <= 2;
+    static constexpr int A = NR == 1 ? 18 : 38;
+    float2 rec[kTileCap];             // candidate positions relative to the group origin
+    uint32_t code[kTileCap];          // (slot << kCodeShift) | image
+    int4 rect[32];                    // per query: cell rectangle at the tile level
+    int32_t rx0[kTileRows], rx1[kTileRows], rpre[kTileRows + 1];
+    int32_t self[32];                 // tile slot of each query's own record
+    uint32_t list[LCAP][32];          // per-query keys, one column per query
+};
+
+__device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t q, int lane) {
+    const uint32_t bal = __ballot_sync(0xffffffffu, mine);
+    if (!bal) return;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(a.D.ndefer, __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (mine) a.D.defer[base + __popc(bal & lanemask_lt())] = (int32_t)q;
+}
+
+template <int MODE, int NR>
+__global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
+    using TS = TileSmem<NR>;
+    constexpr int LCAP = TS::LCAP;
+    constexpr uint32_t FULL = 0xffffffffu;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    TS &sm = reinterpret_cast<TS *>(smem_raw)[w];
+    const int k = a.c.k;
+    const int64_t n = a.c.n;
+    const PArrays &B = a.B;
+    const int64_t ngroups = (n + 31) >> 5;
+    for (int64_t g = (int64_t)blockIdx.x * kTileWarps + w; g < ngroups; g += (int64_t)gridDim.x * kTileWarps) {
+        const int64_t g0 = g << 5;
+        const int64_t q = g0 + lane;
+        const int s0 = sim_of(a.c, g0);
+        const bool valid = q < n && sim_of(a.c, q) == s0;
+        // a group that straddles two simulations of an ensemble searches for
+        // the first one; the other simulation's queries are deferred
+        defer_lanes(a, q < n && !valid, q, lane);
+        const SimDev &S = a.c.sims[s0];
+        const int level = S.level;
+        const int G = 1 << level;
+        const float sx0 = S.fs[0], sy0 = S.fs[1];
+        const float tol = S.tol + S.overshoot;
+        float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
+        float R = 0.f;
+        if (valid) {
+            pr = B.rec[q];
+            R = B.hprev[q] * a.hgrow;
+        }
+        const float pxr = pr.x + pr.z, pyr = pr.y + pr.w;
+        // a radius guess well inside one period (no self image can come within R)
+        const float Rcap = 0.25f * fminf(sx0, sy0) * (float)G;
+        bool defer_all = __any_sync(FULL, valid && !(R > 0.f && R < Rcap));
+        int x0 = INT_MAX, x1 = INT_MIN, y0 = INT_MAX, y1 = INT_MIN;
+        if (valid && !defer_all) {
+            const float Re = R + tol;
+            x0 = (int)floorf((pxr - Re) / sx0);
+            x1 = (int)floorf((pxr + Re) / sx0);
+            y0 = (int)floorf((pyr - Re) / sy0);
+            y1 = (int)floorf((pyr + Re) / sy0);
+            if (S.periodic[0]) { x0 = max(x0, -G); x1 = min(x1, 2 * G - 1); }
+            else { x0 = max(x0, 0); x1 = min(x1, G - 1); }
+            if (S.periodic[1]) { y0 = max(y0, -G); y1 = min(y1, 2 * G - 1); }
+            else { y0 = max(y0, 0); y1 = min(y1, G - 1); }
+        }
+        int sh = 0, BX0 = 0, BX1 = -1, BY0 = 0, BY1 = -1;
+        if (!defer_all) {
+            const int X0 = __reduce_min_sync(FULL, x0), X1 = __reduce_max_sync(FULL, x1);
+            const int Y0 = __reduce_min_sync(FULL, y0), Y1 = __reduce_max_sync(FULL, y1);
+            for (;; sh++) {
+                const int nx = (X1 >> sh) - (X0 >> sh) + 1, ny = (Y1 >> sh) - (Y0 >> sh) + 1;
+                if ((ny <= kTileRows && (int64_t)nx * ny <= kTileBox) || sh == level) {
+                    defer_all = ny > kTileRows || (int64_t)nx * ny > kTileBox;
+                    break;
+                }
+            }
+            BX0 = X0 >> sh; BX1 = X1 >> sh; BY0 = Y0 >> sh; BY1 = Y1 >> sh;
+        }
+        // group origin: the first particle's FP64 position
+        const double2 P = valid ? B.pos[q] : make_double2(0.0, 0.0);
+        const double gx = __shfl_sync(FULL, P.x, 0), gy = __shfl_sync(FULL, P.y, 0);
+        int total = 0;
+        if (!defer_all) {
+            const int shift = level - sh, Gl = 1 << shift;
+            sm.rect[lane] = valid ? make_int4(x0 >> sh, x1 >> sh, y0 >> sh, y1 >> sh) : make_int4(1, 0, 1, 0);
+            sm.self[lane] = -1;
+            __syncwarp();
+            // hull of the query rectangles crossing each row of the box
+            const int ny = BY1 - BY0 + 1;
+            for (int r = lane; r < ny; r += 32) {
+                const int vy = BY0 + r;
+                int hx0 = INT_MAX, hx1 = INT_MIN;
+                for (int j = 0; j < 32; j++) {
+                    const int4 rc = sm.rect[j];
+                    if (rc.z <= vy && vy <= rc.w) { hx0 = min(hx0, rc.x); hx1 = max(hx1, rc.y); }
+                }
+                sm.rx0[r] = hx0;
+                sm.rx1[r] = hx1;
+            }
+            __syncwarp();
+            bool over = false;
+            const double Lx = S.dimg[0], Ly = S.dimg[1];
+            // image blocks: virtual rows / columns below 0 or from Gl on are images
+            for (int wy = BY0 >> shift; wy <= (BY1 >> shift) && !over; wy++) {
+                const int ry0 = max(BY0, wy * Gl) - BY0, ry1 = min(BY1, wy * Gl + Gl - 1) - BY0;
+                const int nrow = ry1 - ry0 + 1;
+                for (int wx = BX0 >> shift; wx <= (BX1 >> shift) && !over; wx++) {
+                    const int xb0 = max(BX0, wx * Gl), xb1 = min(BX1, wx * Gl + Gl - 1);
+                    const uint32_t img = (uint32_t)((1 - wx) * 3 + (1 - wy));
+                    // exclusive prefix of the clipped row widths
+                    int carry = 0;
+                    for (int r0 = 0; r0 < nrow; r0 += 32) {
+                        const int r = r0 + lane;
+                        int wdt = 0;
+                        if (r < nrow) {
+                            const int c0 = max(sm.rx0[ry0 + r], xb0), c1 = min(sm.rx1[ry0 + r], xb1);
+                            wdt = c1 >= c0 ? c1 - c0 + 1 : 0;  // rows no rectangle crosses hold INT_MAX / INT_MIN
+                        }
+                        int inc = wdt;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int y = __shfl_up_sync(FULL, inc, o);
+                            if (lane >= o) inc += y;
+                        }
+                        if (r < nrow) sm.rpre[r] = carry + inc - wdt;
+                        carry += __shfl_sync(FULL, inc, 31);
+                    }
+                    const int ncell = carry;
+                    __syncwarp();
+                    for (int cb = 0; cb < ncell && !over; cb += 32) {
+                        const int c = cb + lane;
+                        int cnt = 0, j0 = 0;
+                        if (c < ncell) {
+                            // the row holding cell c: the last row whose prefix is <= c
+                            int lo = 0, hi = nrow - 1;
+                            while (lo < hi) {
+                                const int mid = (lo + hi + 1) >> 1;
+                                if (sm.rpre[mid] <= c) lo = mid; else hi = mid - 1;
+                            }
+                            const int vy = BY0 + ry0 + lo;
+                            const int vx = max(sm.rx0[ry0 + lo], xb0) + (c - sm.rpre[lo]);
+                            const uint32_t mo = morton2((uint32_t)(vx & (Gl - 1)), (uint32_t)(vy & (Gl - 1)));
+                            j0 = __ldg(a.start + S.cell_off + ((int64_t)mo << (2 * sh)));
+                            cnt = __ldg(a.start + S.cell_off + ((int64_t)(mo + 1) << (2 * sh))) - j0;
+                        }
+                        int inc = cnt;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int y = __shfl_up_sync(FULL, inc, o);
+                            if (lane >= o) inc += y;
+                        }
+                        const int tot = __shfl_sync(FULL, inc, 31);
+                        if (total + tot > kTileCap) {
+                            over = true;
+                            break;
+                        }
+                        const int cbase = j0 - (inc - cnt);  // record t of this chunk is particle cbase + t
+                        for (int t0 = 0; t0 < tot; t0 += 32) {
+                            const int t = t0 + lane;
+                            int src = 0;
+#pragma unroll
+                            for (int b = 16; b > 0; b >>= 1) {
+                                const int iv = __shfl_sync(FULL, inc, src + b - 1);
+                                if (iv <= t) src += b;
+                            }
+                            const int j = __shfl_sync(FULL, cbase, src) + t;
+                            if (t < tot) {
+                                const double2 Q = B.pos[j];
+                                // the image's virtual position (q shifted by wx periods), then
+                                // relative to the group origin, rounded once to FP32
+                                const double qx = wx ? __dadd_rn(Q.x, (double)wx * Lx) : Q.x;
+                                const double qy = wy ? __dadd_rn(Q.y, (double)wy * Ly) : Q.y;
+                                sm.rec[total + t] = make_float2(__double2float_rn(__dsub_rn(qx, gx)),
+                                                                __double2float_rn(__dsub_rn(qy, gy)));
+                                sm.code[total + t] = ((uint32_t)j << kCodeShift) | img;
+                                if (img == 4 && j >= g0 && j < g0 + 32) sm.self[j - g0] = total + t;
+                            }
+                        }
+                        total += tot;
+                    }
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+            defer_all = over || __any_sync(FULL, valid && sm.self[lane] < 0);
+        }
+        if (defer_all) {
+            defer_lanes(a, valid, q, lane);
+            __syncwarp();
+            continue;
+        }
+        // ---- each lane scans the tile for its own query
+        const float rqx = __double2float_rn(__dsub_rn(P.x, gx)), rqy = __double2float_rn(__dsub_rn(P.y, gy));
+        const int myself = sm.self[lane];
+        const float R2 = valid ? R * R : -1.f;
+        const float qs = valid ? 8388608.f / R2 : 0.f;  // key units: R^2 / 2^23
+        int cnt = 0;
+        int t = 0;
+        for (; t + 4 <= total; t += 4) {
+            float2 c[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) c[u] = sm.rec[t + u];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const float dx = c[u].x - rqx, dy = c[u].y - rqy;
+                const float d2 = __fmaf_rn(dx, dx, dy * dy);
+                if (d2 <= R2 && t + u != myself) {
+                    if (cnt < LCAP) {
+                        const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
+                        sm.list[cnt][lane] = (kq << 9) | (uint32_t)(t + u);
+                    }
+                    cnt++;
+                }
+            }
+        }
+        for (; t < total; t++) {
+            const float2 c = sm.rec[t];
+            const float dx = c.x - rqx, dy = c.y - rqy;
+            const float d2 = __fmaf_rn(dx, dx, dy * dy);
+            if (d2 <= R2 && t != myself) {
+                if (cnt < LCAP) {
+                    const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
+                    sm.list[cnt][lane] = (kq << 9) | (uint32_t)t;
+                }
+                cnt++;
+            }
+        }
+        bool ok = valid && cnt >= k && cnt <= LCAP;
+        // decisions in FP32 with the error bound eps
+        const float unit = R2 * 1.1920928955078125e-7f;  // R^2 / 2^23
+        const float ox = pxr - rqx, oy = pyr - rqy;      // group origin in grid coordinates
+        const float Dx = fmaxf(fabsf((float)(BX0 << sh) * sx0 - ox), fabsf((float)((BX1 + 1) << sh) * sx0 - ox));
+        const float Dy = fmaxf(fabsf((float)(BY0 << sh) * sy0 - oy), fabsf((float)((BY1 + 1) << sh) * sy0 - oy));
+        const float ea = kEpsRel * (R2 + 2.f * R * (Dx + Dy)) + 1.8e-15f * S.flmax * R;
+        if (TS::REG) {
+            // the A smallest keys, ascending, by a branch-free insertion chain
+            // per list entry (registers only: no divergence, no smem latency chain)
+            constexpr int A = TS::A;
+            uint32_t arr[A];
+#pragma unroll
+            for (int i = 0; i < A; i++) arr[i] = 0xffffffffu;
+            const int m = ok ? cnt : 0;
+            for (int e = 0; e < m; e++) {
+                uint32_t v = sm.list[e][lane];
+#pragma unroll
+                for (int i = 0; i < A; i++) {
+                    const uint32_t lo = min(arr[i], v);
+                    v = max(arr[i], v);
+                    arr[i] = lo;
+                }
+            }
+            float tau = 0.f, nxt = 3.0e38f, prv = 0.f;
+            bool order_ok = true;
+#pragma unroll
+            for (int i = 0; i < A; i++) {
+                const float ki = (float)(arr[i] >> 9) * unit;
+                if (i == k - 1) tau = ki;
+                if (i == k) nxt = cnt > k ? ki : 3.0e38f;
+                if (i == k - 2) prv = ki;
+                if (MODE != MODE_MIXED && i > 0 && i < k) {
+                    const float kp = (float)(arr[i - 1] >> 9) * unit;
+                    order_ok = order_ok && (ki - kp > 2.f * (kEpsRel * ki + ea));
+                }
+            }
+            const float et = kEpsRel * tau + ea;
+            ok = ok && tau + 3.f * et <= R2 * (1.f - 4.8e-7f);
+            ok = ok && (cnt == k || nxt - tau > 2.f * (kEpsRel * nxt + ea));
+            if (MODE == MODE_MIXED) ok = ok && (k == 1 || tau - prv > 2.f * et);
+            else ok = ok && order_ok;
+            if (ok) {
+                int32_t *out = a.D.nbr + q * k;
+#pragma unroll
+                for (int i = 0; i < A; i++) {
+                    if (i < k) {
+                        const uint32_t slot = arr[i] & 511u;
+                        out[i] = (int32_t)sm.code[slot];
+                        if (MODE == MODE_MIXED) {
+                            const float2 c = sm.rec[slot];
+                            const float dx = c.x - rqx, dy = c.y - rqy;
+                            a.D.d2f[q * k + i] = __fmaf_rn(dx, dx, dy * dy);
+                        }
+                    }
+                }
+            }
+        } else if (ok) {
+            // insertion sort of this lane's keys in its shared-memory column
+            for (int x = 1; x < cnt; x++) {
+                const uint32_t v = sm.list[x][lane];
+                int f = x - 1;
+                uint32_t u = sm.list[f][lane];
+                while (u > v) {
+                    sm.list[f + 1][lane] = u;
+                    if (--f < 0) break;
+                    u = sm.list[f][lane];
+                }
+                sm.list[f + 1][lane] = v;
+            }
+            auto key = [&](int e) { return (float)(sm.list[e][lane] >> 9) * unit; };
+            const float tau = key(k - 1);
+            const float et = kEpsRel * tau + ea;
+            ok = tau + 3.f * et <= R2 * (1.f - 4.8e-7f);
+            if (ok && cnt > k) {
+                const float nx = key(k);
+                ok = nx - tau > 2.f * (kEpsRel * nx + ea);
+            }
+            if (ok) {
+                if (MODE == MODE_MIXED) {
+                    if (k > 1) ok = tau - key(k - 2) > 2.f * et;
+                } else {
+                    float prev = key(0);
+                    for (int e = 1; e < k && ok; e++) {
+                        const float cur = key(e);
+                        ok = cur - prev > 2.f * (kEpsRel * cur + ea);
+                        prev = cur;
+                    }
+                }
+            }
+            if (ok) {
+                int32_t *out = a.D.nbr + q * k;
+                for (int e = 0; e < k; e++) {
+                    const uint32_t slot = sm.list[e][lane] & 511u;
+                    out[e] = (int32_t)sm.code[slot];
+                    if (MODE == MODE_MIXED) {
+                        const float2 c = sm.rec[slot];
+                        const float dx = c.x - rqx, dy = c.y - rqy;
+                        a.D.d2f[q * k + e] = __fmaf_rn(dx, dx, dy * dy);
+                    }
+                }
+            }
+        }
+        defer_lanes(a, valid && !ok, q, lane);
+        __syncwarp();
+    }
 }
 
 // ---------------------------------------------------------------- density
@@ -552,6 +950,8 @@ static size_t knn_smem(int nr) { return (size_t)(kKnnBlock / 32) * 32 * nr * 20;
 template <int MODE, int NR>
 static void knn_attr() {
     cudaFuncSetAttribute(k_knn<MODE, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)knn_smem(NR));
+    cudaFuncSetAttribute(k_knn_tile<MODE, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kTileWarps * sizeof(TileSmem<NR>)));
 }
 template <int MODE>
 static void knn_attrs_mode() {
@@ -575,6 +975,13 @@ static int occ(int) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_knn<MODE, NR>, kKnnBlock, knn_smem(NR));
     return nb;
 }
+template <int MODE, int NR>
+static int occ_tile(int) {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_knn_tile<MODE, NR>, kTileWarps * 32,
+                                                  kTileWarps * sizeof(TileSmem<NR>));
+    return nb;
+}
 
 int knn_occupancy_blocks(int, int cap, int mode) {
     // cap carries k + slack; the list shape follows k
@@ -585,18 +992,46 @@ int knn_occupancy_blocks(int, int cap, int mode) {
     return pick(occ<MODE_MIXED, 1>, occ<MODE_MIXED, 2>, occ<MODE_MIXED, 4>, occ<MODE_MIXED, 8>);
 }
 
+int knn_tile_occupancy_blocks(int k, int mode) {
+    const int nr = list_regs(k);
+    auto pick = [&](auto f1, auto f2, auto f4, auto f8) { return nr == 1 ? f1(0) : nr == 2 ? f2(0) : nr == 4 ? f4(0) : f8(0); };
+    if (mode == MODE_EXACT64)
+        return pick(occ_tile<MODE_EXACT64, 1>, occ_tile<MODE_EXACT64, 2>, occ_tile<MODE_EXACT64, 4>, occ_tile<MODE_EXACT64, 8>);
+    if (mode == MODE_FAST64)
+        return pick(occ_tile<MODE_FAST64, 1>, occ_tile<MODE_FAST64, 2>, occ_tile<MODE_FAST64, 4>, occ_tile<MODE_FAST64, 8>);
+    return pick(occ_tile<MODE_MIXED, 1>, occ_tile<MODE_MIXED, 2>, occ_tile<MODE_MIXED, 4>, occ_tile<MODE_MIXED, 8>);
+}
+
+template <int MODE, int NR>
+static void launch_knn_nr(const KnnArgs &args, const Launch &L, const KnnTune &tune) {
+    const int wpb = kKnnBlock / 32;
+    const size_t smem = knn_smem(NR);
+    const int resident = L.sms * std::max(tune.blocks_per_sm, 1);
+    if (tune.tile && args.D.defer) {
+        // group tiles, then the per-query kernel over the deferred queries
+        cudaMemsetAsync(args.D.ndefer, 0, sizeof(int32_t), L.stream);
+        const int64_t groups = (args.c.n + 31) / 32;
+        const int64_t tneed = (groups + kTileWarps - 1) / kTileWarps;
+        const int tgrid = (int)std::max<int64_t>(
+            1, std::min<int64_t>(tneed, (int64_t)L.sms * std::max(tune.tile_blocks_per_sm, 1)));
+        k_knn_tile<MODE, NR><<<tgrid, kTileWarps * 32, kTileWarps * sizeof(TileSmem<NR>), L.stream>>>(args);
+        KnnArgs d = args;
+        d.use_defer = 1;
+        k_knn<MODE, NR><<<std::max(resident, 1), kKnnBlock, smem, L.stream>>>(d);
+        return;
+    }
+    const int64_t need = (args.c.n + wpb - 1) / wpb;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, resident));
+    k_knn<MODE, NR><<<grid, kKnnBlock, smem, L.stream>>>(args);
+}
+
 template <int MODE>
 static void run_knn(const KnnArgs &args, const Launch &L, const KnnTune &tune) {
     const int nr = list_regs(args.c.k);
-    const int wpb = kKnnBlock / 32;
-    const int64_t need = (args.c.n + wpb - 1) / wpb;
-    int grid = (int)std::min<int64_t>(need, (int64_t)L.sms * std::max(tune.blocks_per_sm, 1));
-    if (grid < 1) grid = 1;
-    const size_t smem = knn_smem(nr);
-    if (nr == 1) k_knn<MODE, 1><<<grid, kKnnBlock, smem, L.stream>>>(args);
-    else if (nr == 2) k_knn<MODE, 2><<<grid, kKnnBlock, smem, L.stream>>>(args);
-    else if (nr == 4) k_knn<MODE, 4><<<grid, kKnnBlock, smem, L.stream>>>(args);
-    else k_knn<MODE, 8><<<grid, kKnnBlock, smem, L.stream>>>(args);
+    if (nr == 1) launch_knn_nr<MODE, 1>(args, L, tune);
+    else if (nr == 2) launch_knn_nr<MODE, 2>(args, L, tune);
+    else if (nr == 4) launch_knn_nr<MODE, 4>(args, L, tune);
+    else launch_knn_nr<MODE, 8>(args, L, tune);
 }
 
 template <int MODE>
@@ -615,6 +1050,7 @@ void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &
     a.start = T.start;
     a.theta = tune.theta;
     a.hgrow = tune.hgrow;
+    a.use_defer = 0;
     if (mode == MODE_EXACT64) run_knn<MODE_EXACT64>(a, L, tune);
     else if (mode == MODE_FAST64) run_knn<MODE_FAST64>(a, L, tune);
     else run_knn<MODE_MIXED>(a, L, tune);

@@ -68,6 +68,29 @@ __global__ void k_scatter_state(Ctx c, PArrays A, const double *x, const double 
     }
 }
 
+// New particles at slots n0 .. n0+count-1 (their caller indices): state from
+// buf (x, y, vx, vy, u blocks of count values), no integrator history.
+__global__ void k_append(PArrays A, int64_t n0, int64_t count, const double *buf) {
+    GRID_STRIDE(i, count) {
+        const int64_t s = n0 + i;
+        const double2 v = make_double2(buf[2 * count + i], buf[3 * count + i]);
+        const double e = buf[4 * count + i];
+        A.pos[s] = make_double2(buf[i], buf[count + i]);
+        A.vel[s] = v;
+        A.vp[s] = v;
+        A.acc[s] = make_double2(0.0, 0.0);
+        A.u[s] = e;
+        A.up[s] = e;
+        A.udot[s] = 0.0;
+        A.id[s] = (int32_t)s;
+        A.hprev[s] = 0.f;
+    }
+}
+
+void launch_append(const Launch &L, const PArrays &A, int64_t n0, int64_t count, const double *buf) {
+    k_append<<<grid_for(L, count, 256), 256, 0, L.stream>>>(A, n0, count, buf);
+}
+
 void launch_scatter_state(const Ctx &c, const Launch &L, const PArrays &A, const double *x,
                           const double *y, const double *vx, const double *vy, const double *u,
                           const double *ax, const double *ay, const double *udot, bool have_acc) {

@@ -138,6 +138,16 @@ class SphConfig:
         return cfg
 
 
+
+def _set_search(h, tiles: bool):
+    L.check(L.load().sph_set_search(h, 1 if tiles else 0))
+
+
+def _search_stats(h) -> tuple:
+    q, d = C.c_int64(), C.c_int64()
+    L.check(L.load().sph_search_stats(h, C.byref(q), C.byref(d)))
+    return q.value, d.value
+
 def _autotune(h, use_cache: bool) -> dict:
     import json
     buf = C.create_string_buffer(1024)
@@ -164,13 +174,20 @@ def MakeConfigFromFile(path: str):
     return SphConfig.from_c(c), None
 
 
-def spawn_start(conf: SphConfig):
-    """Spawn(0) of every [[Start]] spawner: (x, y, vx, vy, u) arrays."""
+def spawn_start(conf: SphConfig, with_keys: bool = False):
+    """Spawn(0) of every [[Start]] spawner: (x, y, vx, vy, u) arrays, and the
+    draw keys Z (Particle.Z) as a sixth array when with_keys."""
     c = conf.to_c()
     n = int(L.load().sph_config_start_count(C.byref(c)))
     arrs = [np.zeros(n) for _ in range(5)]
-    L.check(L.load().sph_config_spawn(C.byref(c), *[L.dptr(a) for a in arrs]))
-    return arrs
+    z = np.zeros(n, np.int64)
+    L.check(L.load().sph_config_spawn(C.byref(c), *[L.dptr(a) for a in arrs], L.i64ptr(z)))
+    return (*arrs, z) if with_keys else arrs
+
+
+def _source_seed(step: int, index: int) -> int:
+    """Generator seed of source `index` at step `step` (deterministic runs)."""
+    return (0x5EED5EED00000000 + (step << 8) + index) & 0xFFFFFFFFFFFFFFFF
 
 
 class Simulation:
@@ -210,8 +227,54 @@ class Simulation:
         return int(L.load().sph_current_step(self._h))
 
     def Step(self, nsteps: int = 1):
-        """sim/sph.go:64 (one call of Step per requested step)."""
-        L.check(L.load().sph_step(self._h, int(nsteps)))
+        """sim/sph.go:64 (one call of Step per requested step). With point
+        sources, each step first appends what they spawn at t = step * dt
+        (sim/sph.go:71-85)."""
+        if not self.Config.Sources:
+            L.check(L.load().sph_step(self._h, int(nsteps)))
+            return
+        for _ in range(int(nsteps)):
+            self._spawn_sources()
+            L.check(L.load().sph_step(self._h, 1))
+
+    def _spawn_sources(self):
+        lib = L.load()
+        step = self.CurrentStep
+        t = float(step) * self.Config.DeltaTHalf * 2
+        for i, src in enumerate(self.Config.Sources):
+            cs = L.SphPointSource((C.c_double * 2)(src.origin.X, src.origin.Y), src.rate, src.LastSpwned)
+            probe = L.SphPointSource.from_buffer_copy(cs)
+            cnt = int(lib.sph_point_source_spawn(C.byref(probe), t, 0, None, None, None, None, None, None))
+            if cnt <= 0:
+                continue
+            x, y, vx, vy, u = (np.zeros(cnt) for _ in range(5))
+            z = np.zeros(cnt, np.int64)
+            got = int(lib.sph_point_source_spawn(C.byref(cs), t, _source_seed(step, i), L.dptr(x), L.dptr(y),
+                                                 L.dptr(vx), L.dptr(vy), L.dptr(u), L.i64ptr(z)))
+            src.LastSpwned = cs.last_spawned
+            L.check(lib.sph_append(self._h, got, L.dptr(x), L.dptr(y), L.dptr(vx), L.dptr(vy), L.dptr(u),
+                                   L.i64ptr(z)))
+            self.n += got
+
+    def SetDrawKeys(self, z):
+        """Particle.Z per particle (caller order) for Frame(); None = caller order."""
+        if z is None:
+            L.check(L.load().sph_set_draw_keys(self._h, None))
+        else:
+            zz = np.ascontiguousarray(z, np.int64)
+            if len(zz) != self.n:
+                raise ValueError("one draw key per particle")
+            L.check(L.load().sph_set_draw_keys(self._h, L.i64ptr(zz)))
+
+    def Frame(self, width: int = 1280, height: int = 720) -> np.ndarray:
+        """sim/animator.go:55-103 CurrentFrame: (height, width, 4) NRGBA bytes."""
+        out = np.empty((height, width, 4), np.uint8)
+        L.check(L.load().sph_render(self._h, width, height, out.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return out
+
+    def FrameToPNG(self, path: str, width: int = 1280, height: int = 720):
+        """sim/animator.go:121-138 FrameToPNG for the current state."""
+        write_png(path, self.Frame(width, height))
 
     def Run(self):
         """sim/sph.go:56-61."""
@@ -226,6 +289,14 @@ class Simulation:
     def Autotune(self, use_cache: bool = True) -> dict:
         """Picks the neighbour search's launch shape for this workload (before the first step)."""
         return _autotune(self._h, use_cache)
+
+    def SetSearch(self, tiles: bool):
+        """Group-tile neighbour search (default) or per-query search; same neighbour sets."""
+        _set_search(self._h, tiles)
+
+    def search_stats(self) -> tuple:
+        """(queries, deferred to the per-query search) of the last force evaluation."""
+        return _search_stats(self._h)
 
     def Save(self, path: str):
         """Checkpoint of the whole integrator state (resumes bit for bit)."""
@@ -280,8 +351,28 @@ class Simulation:
 
 def MakeSimulationFromConf(conf: SphConfig) -> Simulation:
     """sim/sph.go:41-54: spawns the [[Start]] particles and builds the simulation."""
-    x, y, vx, vy, u = spawn_start(conf)
-    return Simulation(conf, x, y, vx, vy, u)
+    x, y, vx, vy, u, z = spawn_start(conf, with_keys=True)
+    sim = Simulation(conf, x, y, vx, vy, u)
+    sim.SetDrawKeys(z)
+    return sim
+
+
+def write_png(path: str, rgba: np.ndarray):
+    """8-bit RGBA PNG (what image/png writes for an opaque NRGBA image holds
+    the same pixels)."""
+    import struct
+    import zlib
+    h, w = rgba.shape[:2]
+    raw = b"".join(b"\x00" + rgba[r].tobytes() for r in range(h))
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))
 
 
 def MakeSimulation() -> Simulation:
@@ -333,6 +424,12 @@ class Ensemble:
 
     def Autotune(self, use_cache: bool = True) -> dict:
         return _autotune(self._h, use_cache)
+
+    def SetSearch(self, tiles: bool):
+        _set_search(self._h, tiles)
+
+    def search_stats(self) -> tuple:
+        return _search_stats(self._h)
 
     def state(self) -> dict:
         names = ["x", "y", "vx", "vy", "u", "ax", "ay", "udot"]

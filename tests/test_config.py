@@ -160,7 +160,7 @@ def test_point_source_rate(sphlib):
     src.rate = 10.0
     lib = L.load()
     x, y = np.empty(8), np.empty(8)
-    n = lib.sph_point_source_spawn(C.byref(src), 0.35, 1, L.dptr(x), L.dptr(y), None, None, None)
+    n = lib.sph_point_source_spawn(C.byref(src), 0.35, 1, L.dptr(x), L.dptr(y), None, None, None, None)
     assert n == 3 and src.last_spawned == pytest.approx(0.3)
     assert np.all(np.abs(x[:3] - 0.5) <= 0.01)
-    assert lib.sph_point_source_spawn(C.byref(src), 0.45, 2, None, None, None, None, None) == 1
+    assert lib.sph_point_source_spawn(C.byref(src), 0.45, 2, None, None, None, None, None, None) == 1

@@ -74,7 +74,7 @@ def test_autotune_keeps_results_and_caches(gpu, tmp_path, monkeypatch, precision
     c = _sim(12_000, precision)
     rep2 = c.Autotune(use_cache=True)
     assert rep2["cached"] is True and rep2["theta"] == rep["theta"] and rep2["level_delta"] == rep["level_delta"]
-    assert (tmp_path / "tune.txt").read_text().count("sphgpu-tune-v1") == 1
+    assert (tmp_path / "tune.txt").read_text().count("sphgpu-tune-v2") == 1
 
 
 @pytest.mark.parametrize("precision", ["Exact", "Mixed"])
@@ -112,3 +112,47 @@ def test_division_sequences_are_correctly_rounded(gpu):
     bad = C.c_int64(-1)
     L.check(gpu.sph_selftest_division(200_000_000, 12345, C.byref(bad)))
     assert bad.value == 0
+
+
+@pytest.mark.parametrize("precision", ["Exact", "Mixed"])
+def test_group_tiles_match_per_query_search(gpu, precision):
+    """The group-tile search (default) and the per-query search return the
+    same exact neighbour sets; in the FP64 form every result is identical."""
+    a, b = _sim(30_000, precision), _sim(30_000, precision)
+    b.SetSearch(False)
+    if precision == "Exact":
+        a.Step(5)
+        b.Step(5)
+        sa, sb = a.state(), b.state()
+        for key in sa:
+            assert np.array_equal(sa[key], sb[key]), key
+    else:
+        # the first evaluation has no previous smoothing lengths (per-query
+        # search in both); the second, on the same positions, runs the tiles in a
+        for _ in range(2):
+            a.CalculateForces()
+            b.CalculateForces()
+        ia, da, ma = a.neighbours()
+        ib, db, mb = b.neighbours()
+        assert np.array_equal(ia, ib) and np.array_equal(da, db) and np.array_equal(ma, mb)
+        assert np.allclose(a.derived()["rho"], b.derived()["rho"], rtol=1e-5, atol=0)  # the mixed tolerance
+    qa, dfa = a.search_stats()
+    qb, dfb = b.search_stats()
+    assert qa == qb == 30_000 and dfb == qb
+    assert dfa < 0.2 * qa  # most queries settled by the tiles
+
+
+def test_group_tiles_cover_ensemble_boundaries_and_images(gpu):
+    """Groups that straddle two simulations of an ensemble, and tiles that
+    reach across the periodic boundary, give the same results as the per-query
+    search."""
+    confs, arrays = ics.make_ensemble(nsims=12, seed=3, precision="Exact")
+    e1, e2 = S.Ensemble(confs, arrays), S.Ensemble(confs, arrays)
+    e2.SetSearch(False)
+    e1.Step(4)
+    e2.Step(4)
+    s1, s2 = e1.state(), e2.state()
+    for key in s1:
+        assert np.array_equal(s1[key], s2[key]), key
+    q, d = e1.search_stats()
+    assert d < q
