@@ -438,6 +438,7 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
             return bail(fail(SPH_ERR_CUDA, "device initialisation failed"));
     }
     knn_init_attrs();
+    force_init_attrs((int)k);
     h->tune.block = 256;
     h->tune.cap = (int)(k + 16);
     h->tune.theta = 0.5f;

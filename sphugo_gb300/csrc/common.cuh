@@ -224,6 +224,7 @@ void knn_init_attrs();
 void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D,
                 const Tables &T, int mode, const KnnTune &tune);
 void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode);
+void force_init_attrs(int k);
 void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays &A,
                   const Derived &D, int mode, bool integrate);
 

@@ -6,6 +6,8 @@
 // neighbours' predicted velocity, sound speed, density and smoothing length.
 #include "physics.cuh"
 
+#include <algorithm>
+
 namespace sphgpu {
 
 struct ForceArgs {
@@ -202,6 +204,201 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
     if (fl) atomicOr(a.c.flags, fl);
 }
 
+// ---------------------------------------------------------------- FP64 form,
+// viscosity compacted. One warp per 32 consecutive particles, one lane per
+// particle, in three phases:
+//   1. each lane flags its approaching neighbour pairs (v_AB . r_AB < 0);
+//   2. the warp computes the viscosity term Pi of every flagged pair of its
+//      32 particles with all lanes busy (the pairs dealt out in turn) and
+//      keeps them in shared memory;
+//   3. each lane sums its k terms farthest first (sim/sph.go:343-392), taking
+//      Pi from shared memory for the flagged pairs.
+// Phase 3 is the reference's loop with Pi looked up instead of computed in a
+// branch that a warp runs whenever any of its lanes needs it; every operation
+// and its order are unchanged, so the results stay bit-exact.
+constexpr int kForceWarps = 4;
+
+// per-warp shared memory: Pi doubles, masks, counts; rounded up to 16 bytes
+// so that every warp's Pi array starts 8-byte (in fact 16-byte) aligned
+__host__ __device__ constexpr size_t force_exact_warp_bytes(int k) {
+    return ((size_t)k * 256 + 4 * 32 * 4 + 33 * 4 + 15) & ~(size_t)15;
+}
+constexpr bool force_exact_layout_aligned() {
+    for (int k = 1; k <= 128; k++)
+        if (force_exact_warp_bytes(k) % 16 != 0 || ((size_t)k * 256) % 8 != 0) return false;
+    return true;
+}
+static_assert(force_exact_layout_aligned(), "per-warp shared-memory regions must stay 16-byte aligned");
+
+// r_AB = (q - offset) - p and v_AB . r_AB for neighbour code `code` of a
+// particle at P with predicted velocity vpi (sim/sph.go:355-367)
+__device__ __forceinline__ void pair_geom(const SimDev &S, const PArrays &B, uint32_t code, double2 P, double2 vpi,
+                                          double &rabx, double &raby, double &dot) {
+    const uint32_t j = code >> kCodeShift;
+    const double2 vpj = B.vp[j];
+    const double vabx = __dsub_rn(vpj.x, vpi.x), vaby = __dsub_rn(vpj.y, vpi.y);
+    const double2 Q = B.pos[j];
+    if ((code & 15u) == 4u) {  // q - 0 = q exactly
+        rabx = __dsub_rn(Q.x, P.x);
+        raby = __dsub_rn(Q.y, P.y);
+    } else {
+        double ox, oy;
+        img_shift(S, code & 15u, ox, oy);
+        rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
+        raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
+    }
+    dot = __dadd_rn(__dmul_rn(vabx, rabx), __dmul_rn(vaby, raby));
+}
+
+__global__ void __launch_bounds__(kForceWarps * 32) k_force_exact(ForceArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int k = a.c.k;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nw = (k + 31) >> 5;  // mask words per particle (k <= 128)
+    // per warp: Pi[k][32] doubles, approach masks [4][32], inclusive pair counts [33]
+    unsigned char *wb = smem_raw + (size_t)w * force_exact_warp_bytes(k);
+    double *spi = (double *)wb;
+    uint32_t *smask = (uint32_t *)(wb + (size_t)k * 256);
+    int32_t *sinc = (int32_t *)(smask + 4 * 32);
+    const PArrays &B = a.B;
+    const Derived &D = a.D;
+    unsigned fl = 0;
+    const int64_t n = a.c.n;
+    for (int64_t q0 = ((int64_t)blockIdx.x * kForceWarps + w) * 32; q0 < n;
+         q0 += (int64_t)gridDim.x * kForceWarps * 32) {
+        const int64_t q = q0 + lane;
+        const bool valid = q < n;
+        const SimDev &S = a.c.sims[valid ? sim_of(a.c, q) : 0];
+        double2 P = make_double2(0.0, 0.0), vpi = P;
+        double4 di = make_double4(0.0, 0.0, 0.0, 0.0);
+        const int32_t *nb = D.nbr + q * k;
+        // ---- 1. approaching pairs
+        int cnt = 0;
+        if (valid) {
+            P = B.pos[q];
+            vpi = B.vp[q];
+            di = D.der[q];
+            for (int wd = 0; wd < nw; wd++) {
+                uint32_t m = 0;
+                const int e1 = min(k, (wd + 1) * 32);
+                for (int e = wd * 32; e < e1; e++) {
+                    double rabx, raby, dot;
+                    pair_geom(S, B, (uint32_t)nb[e], P, vpi, rabx, raby, dot);
+                    if (dot < 0.0) m |= 1u << (e & 31);
+                }
+                smask[wd * 32 + lane] = m;
+                cnt += __popc(m);
+            }
+        } else {
+            for (int wd = 0; wd < nw; wd++) smask[wd * 32 + lane] = 0u;
+        }
+        int inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        sinc[lane] = inc;
+        const int total = __shfl_sync(0xffffffffu, inc, 31);
+        __syncwarp();
+        // ---- 2. Pi of every flagged pair of the warp's particles
+        for (int i = lane; i < total; i += 32) {
+            int p = 0;  // owner: the first lane whose inclusive count exceeds i
+#pragma unroll
+            for (int b = 16; b > 0; b >>= 1)
+                if (sinc[p + b - 1] <= i) p += b;
+            int r = i - (p ? sinc[p - 1] : 0);  // r-th flagged pair of particle p
+            int e = 0;
+            for (int wd = 0; wd < nw; wd++) {
+                uint32_t m = smask[wd * 32 + p];
+                const int c = __popc(m);
+                if (r < c) {
+                    for (int t = 0; t < r; t++) m &= m - 1;
+                    e = wd * 32 + __ffs(m) - 1;
+                    break;
+                }
+                r -= c;
+            }
+            const int64_t qp = q0 + p;
+            const SimDev &Sp = a.c.sims[sim_of(a.c, qp)];
+            const double2 Pp = B.pos[qp], vpp = B.vp[qp];
+            const double4 dp = D.der[qp];
+            const uint32_t code = (uint32_t)D.nbr[qp * k + e];
+            double rabx, raby, dot;
+            pair_geom(Sp, B, code, Pp, vpp, rabx, raby, dot);
+            const double4 dj = D.der[code >> kCodeShift];
+            const double cab = __dmul_rn(0.5, __dadd_rn(dp.x, dj.x));
+            const double rhoab = __dmul_rn(0.5, __dadd_rn(dp.y, dj.y));
+            const double hab = __dmul_rn(0.5, __dadd_rn(dp.z, dj.z));
+            const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
+            const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, Sp.etasq));
+            spi[e * 32 + p] = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-Sp.alpha, cab), mu),
+                                                  __dmul_rn(__dmul_rn(Sp.beta, mu), mu)),
+                                        rhoab);
+        }
+        __syncwarp();
+        // ---- 3. the reference's ordered sums
+        if (valid) {
+            const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
+            (void)ci;
+            (void)rhoi;
+            const double2 *dist = D.dist + q * k;
+            double ax = 0.0, ay = 0.0, ed = 0.0;
+            for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
+                const uint32_t code = (uint32_t)nb[e];
+                const double d = dist[e].x;
+                const double qq = dist[e].y;  // NNDists[i]/maxR, the density pass's identical quotient
+                const double drk = kdf_exact(S.kernel, qq);
+                double rabx, raby, dot;
+                pair_geom(S, B, code, P, vpi, rabx, raby, dot);
+                const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;
+                const double piab = visc ? spi[e * 32 + lane] : 0.0;
+                const double cb = D.der[code >> kCodeShift].w;
+                const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
+                // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
+                const double yd = __drcp_rn(d);
+                ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
+                ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
+                ed = __dadd_rn(ed, __dmul_rn(dot, drk));
+            }
+            const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
+            const double axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
+            const double ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
+            const double edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
+            if (!isfinite(axo) || !isfinite(ayo) || !isfinite(edot)) fl |= FLAG_Q_RANGE;
+            double2 pos = P, vel = B.vel[q];
+            double u = B.u[q];
+            if (a.integrate) integrate_one(S, pos, vel, u, axo, ayo, edot);
+            a.A.pos[q] = pos;
+            a.A.vel[q] = vel;
+            a.A.u[q] = u;
+            a.A.acc[q] = make_double2(axo, ayo);
+            a.A.udot[q] = edot;
+            a.A.id[q] = B.id[q];
+            a.A.hprev[q] = (float)D.h[q];
+            a.A.vp[q] = vpi;
+            a.A.up[q] = B.up[q];
+        }
+        __syncwarp();
+    }
+    if (fl) atomicOr(a.c.flags, fl);
+}
+
+static size_t force_exact_smem(int k) { return (size_t)kForceWarps * force_exact_warp_bytes(k); }
+
+static int g_force_exact_blocks[129];  // resident blocks per SM by k (filled before any capture)
+
+// Sets the shared-memory limit of the FP64 force kernel and records its
+// occupancy for k; must run before any stream capture.
+void force_init_attrs(int k) {
+    cudaFuncSetAttribute(k_force_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_exact_smem(128));
+    if (k >= 1 && k <= 128 && !g_force_exact_blocks[k]) {
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_exact, kForceWarps * 32, force_exact_smem(k));
+        g_force_exact_blocks[k] = std::max(nb, 1);
+    }
+}
+
 void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays &A,
                   const Derived &D, int mode, bool integrate) {
     ForceArgs a;
@@ -214,8 +411,13 @@ void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays
     int64_t need = (c.n + block - 1) / block;
     int grid = (int)(need < (int64_t)L.sms * 16 ? need : (int64_t)L.sms * 16);
     if (grid < 1) grid = 1;
-    if (mode == MODE_EXACT64) k_force<MODE_EXACT64><<<grid, block, 0, L.stream>>>(a);
-    else if (mode == MODE_FAST64) k_force<MODE_FAST64><<<grid, block, 0, L.stream>>>(a);
+    if (mode == MODE_EXACT64) {
+        const int64_t tiles = (c.n + 31) / 32;
+        const int64_t eneed = (tiles + kForceWarps - 1) / kForceWarps;
+        const int nb = c.k >= 1 && c.k <= 128 ? std::max(g_force_exact_blocks[c.k], 1) : 1;
+        const int eg = (int)std::max<int64_t>(1, std::min<int64_t>(eneed, (int64_t)L.sms * nb));
+        k_force_exact<<<eg, kForceWarps * 32, force_exact_smem(c.k), L.stream>>>(a);
+    } else if (mode == MODE_FAST64) k_force<MODE_FAST64><<<grid, block, 0, L.stream>>>(a);
     else k_force<MODE_MIXED><<<grid, block, 0, L.stream>>>(a);
 }
 

@@ -852,9 +852,14 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
 // ---------------------------------------------------------------- density
 // the reference's squared distance to the neighbour image a list code names
 __device__ __forceinline__ double nbr_d2(const SimDev &S, const PArrays &B, double2 P, uint32_t code) {
+    const double2 Q = B.pos[code >> kCodeShift];
+    if ((code & 15u) == 4u) {
+        // no offset: p + 0 = p (and -0 + 0 = +0 squares to the same value)
+        const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
+        return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    }
     double ox, oy;
     img_shift(S, code & 15u, ox, oy);
-    const double2 Q = B.pos[code >> kCodeShift];
     return dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
 }
 
@@ -882,12 +887,13 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             double acc = 0.0;
             for (int e = k - 1; e >= 0; e--) {
                 const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, (uint32_t)nb[e]));
-                const double x = div_rn_recip(d, h, yh);  // == __ddiv_rn(d, h)
-                if (x > 1.0 || x < 0.0) fl |= FLAG_Q_RANGE;
+                // == __ddiv_rn(d, h); in [0, 1] because the list is sorted (d <= h)
+                const double x = div_rn_recip(d, h, yh);
                 acc = __dadd_rn(acc, kf_exact(S.kernel, x));
                 dist[e] = make_double2(d, x);  // NNDists and q = NNDists/h for the force
             }
             rho = __ddiv_rn(__dmul_rn(__dmul_rn(S.fpref, S.mass), acc), __dmul_rn(h, h));
+            if (!(rho >= 0.0 && rho < 1.0e308)) fl |= FLAG_Q_RANGE;  // a NaN or infinite distance
             cs = __dsqrt_rn(__dmul_rn(__dmul_rn(gamma, __dsub_rn(gamma, 1.0)), up));
             cterm = __ddiv_rn(__dmul_rn(cs, cs), __dmul_rn(gamma, rho));
         } else if (MODE == MODE_FAST64) {
