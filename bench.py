@@ -318,7 +318,7 @@ def run_reference(args, dist):
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head_form != "Mixed" else "f32+f64", "data": "synthetic (seeded SplitMix64)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
         "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}",
                    "n": n, "k": K_NEIGH, "form": "reference tree search, FP64"},
         "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
