@@ -153,7 +153,7 @@ int alloc_parrays(sph_handle *h, PArrays &P, bool mixed, int64_t n) {
     rc |= dalloc(h, &P.id, n);
     rc |= dalloc(h, &P.hprev, n);
     rc |= dalloc(h, &P.rec, n);
-    if (mixed) rc |= dalloc(h, &P.vrec, n);
+    rc |= dalloc(h, &P.vrec, n);  // predicted velocities as float pairs (mixed sums, FP64 force's sign test)
     return rc ? SPH_ERR_NOMEM : SPH_OK;
 }
 
@@ -285,7 +285,7 @@ void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) 
     launch_scan(c, L, h->T);
     launch_stable(c, L, h->T);
     mark(2);
-    launch_permute(c, L, h->A, h->B, h->T, pred, h->mode == MODE_MIXED);
+    launch_permute(c, L, h->A, h->B, h->T, pred, h->mode != MODE_FAST64);
     mark(3);
     launch_knn(c, L, h->B, h->D, h->T, h->mode, h->tune);
     mark(4);

@@ -62,6 +62,7 @@ struct SimDev {
     float fs[2];           // finest cell side
     float fimg_h[2], fimg_l[2]; // image shifts as float pairs (hi, lo)
     float flmax;           // max(L)
+    float fmag;            // bound on |p + offset| of any particle image (the reference rounds it)
     unsigned long long bbox[4]; // open axes: ordered-key min x, max x, min y, max y
 };
 
@@ -154,6 +155,13 @@ __host__ __device__ inline void simdev_floats(SimDev &S) {
         S.fimg_l[a] = (float)(S.dimg[a] - (double)S.fimg_h[a]);
     }
     S.flmax = (float)(S.L[0] > S.L[1] ? S.L[0] : S.L[1]);
+    double mag = 0.0;
+    for (int a = 0; a < 2; a++) {
+        const double lo = S.lo[a] < 0 ? -S.lo[a] : S.lo[a], hi = S.lo[a] + S.L[a] < 0 ? -(S.lo[a] + S.L[a]) : S.lo[a] + S.L[a];
+        const double m = (lo > hi ? lo : hi) + S.L[a] + (S.dimg[a] < 0 ? -S.dimg[a] : S.dimg[a]);
+        mag = m > mag ? m : mag;
+    }
+    S.fmag = (float)mag;
 }
 
 // order-preserving 64-bit key of a double (for atomic min/max)

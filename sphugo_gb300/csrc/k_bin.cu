@@ -240,7 +240,8 @@ void launch_stable(const Ctx &c, const Launch &L, const Tables &T) {
 // --------------------------------------------------------------- permute
 // Writes the predicted state into cell order (B), plus the float-pair
 // position record relative to the grid origin used by the FP32 distance
-// filter and the mixed-precision sums.
+// filter and the mixed-precision sums, and (vel_records) the predicted
+// velocity as float pairs.
 __global__ void k_permute(Ctx c, PArrays A, PArrays B, Tables T, int pred, int mixed) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.n;
          i += (int64_t)gridDim.x * blockDim.x) {

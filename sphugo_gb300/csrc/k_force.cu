@@ -272,19 +272,46 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_exact(ForceArgs a) {
         double2 P = make_double2(0.0, 0.0), vpi = P;
         double4 di = make_double4(0.0, 0.0, 0.0, 0.0);
         const int32_t *nb = D.nbr + q * k;
-        // ---- 1. approaching pairs
+        // ---- 1. approaching pairs: the sign of v_AB . r_AB from the float-pair
+        // records, with an error bound; the reference's FP64 dot product only
+        // where the bound cannot decide (e.g. equal velocities)
         int cnt = 0;
         if (valid) {
             P = B.pos[q];
             vpi = B.vp[q];
             di = D.der[q];
+            const float4 pr = B.rec[q], vi = B.vrec[q];
+            const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
+            const float lbig = 2.f * fmaxf(S.flmax, S.fmag);
             for (int wd = 0; wd < nw; wd++) {
                 uint32_t m = 0;
                 const int e1 = min(k, (wd + 1) * 32);
                 for (int e = wd * 32; e < e1; e++) {
-                    double rabx, raby, dot;
-                    pair_geom(S, B, (uint32_t)nb[e], P, vpi, rabx, raby, dot);
-                    if (dot < 0.0) m |= 1u << (e & 31);
+                    const uint32_t code = (uint32_t)nb[e];
+                    const uint32_t j = code >> kCodeShift;
+                    const int ia = (int)((code & 15u) / 3u) - 1, ib = (int)((code & 15u) % 3u) - 1;
+                    const float4 r = B.rec[j], vj = B.vrec[j];
+                    const float rx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
+                                     (r.z - (pr.z + (float)ia * dXl));
+                    const float ry = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
+                                     (r.w - (pr.w + (float)ib * dYl));
+                    const float vx = (vj.x - vi.x) + (vj.z - vi.z), vy = (vj.y - vi.y) + (vj.w - vi.w);
+                    const float px = vx * rx, py = vy * ry;
+                    const float dotf = px + py;
+                    // |dotf - reference dot| bound: float-pair residues (2^-48 relative
+                    // to |p|, |v|), FP32 differences, products and sum (2^-23 each)
+                    const float vmag = fabsf(vj.x) + fabsf(vi.x) + fabsf(vj.y) + fabsf(vi.y);
+                    const float eb = 9.5367431640625e-7f * (fabsf(px) + fabsf(py)) +
+                                     9.094947017729282e-13f * (lbig * (fabsf(vx) + fabsf(vy)) + vmag * (fabsf(rx) + fabsf(ry)));
+                    bool approach;
+                    if (dotf < -eb) approach = true;
+                    else if (dotf > eb) approach = false;
+                    else {
+                        double rabx, raby, dot;
+                        pair_geom(S, B, code, P, vpi, rabx, raby, dot);
+                        approach = dot < 0.0;
+                    }
+                    if (approach) m |= 1u << (e & 31);
                 }
                 smask[wd * 32 + lane] = m;
                 cnt += __popc(m);

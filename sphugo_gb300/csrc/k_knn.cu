@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
         const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
         const int64_t coff = S.cell_off;
         const float Lmax = S.flmax;
-        const float epsabs = 1.8e-15f * Lmax;
+        const float epsabs = 1.8e-15f * fmaxf(Lmax, S.fmag);  // the reference's rounding of p + offset
         // per-image constants of the float-pair difference (q - offset) - p
         const float axm = pr.x - dXh, aym = pr.y - dYh;
         const float cxp = pr.z + dXl, cxm = pr.z - dXl, cyp = pr.w + dYl, cym = pr.w - dYl;
@@ -747,7 +747,7 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
         const float ox = pxr - rqx, oy = pyr - rqy;      // group origin in grid coordinates
         const float Dx = fmaxf(fabsf((float)(BX0 << sh) * sx0 - ox), fabsf((float)((BX1 + 1) << sh) * sx0 - ox));
         const float Dy = fmaxf(fabsf((float)(BY0 << sh) * sy0 - oy), fabsf((float)((BY1 + 1) << sh) * sy0 - oy));
-        const float ea = kEpsRel * (R2 + 2.f * R * (Dx + Dy)) + 1.8e-15f * S.flmax * R;
+        const float ea = kEpsRel * (R2 + 2.f * R * (Dx + Dy)) + 1.8e-15f * fmaxf(S.flmax, S.fmag) * R;
         if (TS::REG) {
             // the A smallest keys, ascending, by a branch-free insertion chain
             // per list entry (registers only: no divergence, no smem latency chain)

@@ -106,6 +106,20 @@ def test_non_unit_periodic_box(gpu, oracle):
     assert_bitwise(g, o)
 
 
+def test_periodic_box_far_from_the_origin(gpu, oracle):
+    """Large absolute coordinates: the reference's rounding of p + offset is
+    no longer small against the box; neighbour sets and states stay exact."""
+    n = 2000
+    x, y, vx, vy, u = ics.uniform_blast(n, 13)
+    x, y = 1000.0 + x, -3000.0 + 2.0 * y
+    conf = S.SphConfig(DeltaTHalf=1e-4, Gamma=5 / 3, ParticleMass=1.0 / n, HorPeriodicity=(1000.0, 1001.0),
+                       VertPeriodicity=(-3000.0, -2998.0), ViscosityAlpha=1.0, ViscosityBeta=2.0)
+    g, o = pair(oracle, conf, (x, y, vx, vy, u))
+    g.Step(6)
+    o.step(6)
+    assert_bitwise(g, o)
+
+
 def test_lattice_ties_broken_by_id_and_image(gpu, oracle):
     G = 20
     i, j = np.meshgrid(np.arange(G), np.arange(G), indexing="ij")
