@@ -40,8 +40,10 @@ __device__ __forceinline__ void integrate_one(const SimDev &S, double2 &pos, dou
     if (pos.y > S.refl[3]) { pos.y = __dsub_rn(pos.y, __dsub_rn(pos.y, S.refl[3])); vel.y = -vel.y; }
 }
 
+// The fast-FP64 and mixed forms (the FP64 form is k_force_exact below).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
+    static_assert(MODE != MODE_EXACT64, "the FP64 form runs k_force_exact");
     const int k = a.c.k;
     const PArrays &B = a.B;
     const Derived &D = a.D;
@@ -53,49 +55,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
         const double2 P = B.pos[q];
         const int32_t *nb = D.nbr + q * k;
         double axo, ayo, edot;
-        if (MODE == MODE_EXACT64) {
-            const double4 di = D.der[q];
-            const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
-            const double2 vpi = B.vp[q];
-            const double2 *dist = D.dist + q * k;
-            double ax = 0.0, ay = 0.0, ed = 0.0;
-            for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
-                const uint32_t code = (uint32_t)nb[e];
-                const uint32_t j = code >> kCodeShift;
-                const double d = dist[e].x;
-                const double qq = dist[e].y;  // NNDists[i]/maxR, the density pass's identical quotient
-                const double drk = kdf_exact(S.kernel, qq);
-                const double4 dj = D.der[j];
-                const double2 vpj = B.vp[j];
-                const double vabx = __dsub_rn(vpj.x, vpi.x), vaby = __dsub_rn(vpj.y, vpi.y);
-                double ox, oy;
-                img_shift(S, code & 15u, ox, oy);
-                const double2 Q = B.pos[j];
-                const double rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
-                const double raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
-                const double dot = __dadd_rn(__dmul_rn(vabx, rabx), __dmul_rn(vaby, raby));
-                double piab = 0.0;
-                if (dot < 0.0) {
-                    const double cab = __dmul_rn(0.5, __dadd_rn(ci, dj.x));
-                    const double rhoab = __dmul_rn(0.5, __dadd_rn(rhoi, dj.y));
-                    const double hab = __dmul_rn(0.5, __dadd_rn(hi, dj.z));
-                    const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
-                    const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, S.etasq));
-                    piab = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-S.alpha, cab), mu),
-                                               __dmul_rn(__dmul_rn(S.beta, mu), mu)), rhoab);
-                }
-                const double sum3 = __dadd_rn(__dadd_rn(piab, ca), dj.w);
-                // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
-                const double yd = __drcp_rn(d);
-                ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
-                ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
-                ed = __dadd_rn(ed, __dmul_rn(dot, drk));
-            }
-            const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
-            axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
-            ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
-            edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
-        } else if (MODE == MODE_FAST64) {
+        if (MODE == MODE_FAST64) {
             const double4 di = D.der[q];
             const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
             const double inv_h = 1.0 / hi;
@@ -374,8 +334,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_exact(ForceArgs a) {
             for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
                 const uint32_t code = (uint32_t)nb[e];
                 const double d = dist[e].x;
-                const double qq = dist[e].y;  // NNDists[i]/maxR, the density pass's identical quotient
-                const double drk = kdf_exact(S.kernel, qq);
+                const double drk = dist[e].y;  // dF(NNDists[i]/maxR), evaluated by the density pass
                 double rabx, raby, dot;
                 pair_geom(S, B, code, P, vpi, rabx, raby, dot);
                 const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;

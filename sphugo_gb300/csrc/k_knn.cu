@@ -884,13 +884,40 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
             const double yh = __drcp_rn(h);  // RN(1/h), shared by the k quotients d/h
-            double acc = 0.0;
+            // NNDists and q = NNDists/h; q grows with e (the list is sorted), so
+            // the entries with q < 0.5 are a prefix of length s
+            int s_lo = 0;
             for (int e = k - 1; e >= 0; e--) {
                 const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, (uint32_t)nb[e]));
-                // == __ddiv_rn(d, h); in [0, 1] because the list is sorted (d <= h)
+                // == __ddiv_rn(d, h); in [0, 1] because d <= h
                 const double x = div_rn_recip(d, h, yh);
-                acc = __dadd_rn(acc, kf_exact(S.kernel, x));
-                dist[e] = make_double2(d, x);  // NNDists and q = NNDists/h for the force
+                s_lo += __double_as_longlong(x) < __double_as_longlong(0.5);  // x < 0.5 (x >= 0)
+                dist[e] = make_double2(d, x);
+            }
+            // kernel sums farthest first (sim/sph.go:311-316), each branch of the
+            // Monahan kernel in its own loop (no divergent branch per term); the
+            // force's dF(q) replaces q in the list
+            double acc = 0.0;
+            if (S.kernel == SPH_KERNEL_WENDLAND) {
+                for (int e = k - 1; e >= 0; e--) {
+                    const double x = dist[e].y;
+                    acc = __dadd_rn(acc, kf_exact(SPH_KERNEL_WENDLAND, x));
+                    dist[e].y = kdf_exact(SPH_KERNEL_WENDLAND, x);
+                }
+            } else {
+                for (int e = k - 1; e >= s_lo; e--) {  // q >= 0.5
+                    const double x = dist[e].y;
+                    const double a1 = __dsub_rn(1.0, x);
+                    const double a2 = __dmul_rn(a1, a1);
+                    acc = __dadd_rn(acc, div3_rn(__dmul_rn(a2, a1)));
+                    dist[e].y = -a2;
+                }
+                for (int e = s_lo - 1; e >= 0; e--) {  // q < 0.5
+                    const double x = dist[e].y;
+                    const double qq = __dmul_rn(x, x);
+                    acc = __dadd_rn(acc, __dadd_rn(__dsub_rn(__dmul_rn(qq, x), qq), 1.0 / 6.0));
+                    dist[e].y = __dsub_rn(__dmul_rn(__dmul_rn(3.0, x), x), __dmul_rn(2.0, x));
+                }
             }
             rho = __ddiv_rn(__dmul_rn(__dmul_rn(S.fpref, S.mass), acc), __dmul_rn(h, h));
             if (!(rho >= 0.0 && rho < 1.0e308)) fl |= FLAG_Q_RANGE;  // a NaN or infinite distance
