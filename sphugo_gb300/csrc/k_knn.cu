@@ -483,22 +483,24 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
 //   2. each row of the box keeps the hull of the query rectangles crossing
 //      it; the cells of those row hulls are contiguous particle ranges of the
 //      sorted order, copied once into a shared-memory tile as FP32 positions
-//      relative to the group's first particle (image shift applied in FP64
-//      before the rounding) with their neighbour codes;
+//      relative to the group's first particle (from the float-pair records;
+//      for periodic images the shift is applied in FP64 before the rounding)
+//      with their neighbour codes;
 //   3. each lane scans the whole tile for its own query (broadcast reads) and
 //      keeps every record within R as a 32-bit key: the squared distance in
 //      units of R^2 / 2^23 (23 bits) above the tile slot (9 bits);
 //   4. each lane keeps its k+1 smallest keys in ascending order (a
 //      branch-free insertion chain in registers; an insertion sort in its
-//      shared-memory column for k > 37) and accepts the first k when the FP32
+//      shared-memory column for k > 80) and accepts the first k when the FP32
 //      values decide them:
 //      the k-th lies 3 eps inside R (the tile held every candidate), the
 //      (k+1)-th lies more than 2 eps beyond it (the set), and in the FP64
 //      forms every neighbour is more than 2 eps from the next (the order;
 //      the mixed form needs only the farthest to be unique, it fixes h).
 // eps bounds |FP32 key - reference FP64 squared distance|: 2^-20 d2 for the
-// products, 2^-20 D R for the relative coordinates (|coordinate| <= D),
-// 2^-21 R^2 for the 23-bit key, and the reference's own rounding of p + offset.
+// products, 2^-19 D R for the relative coordinates (|coordinate| <= D, float
+// pair differences), 2^-20 R^2 for the 23-bit key, and 2^-42 L R for the
+// float-pair residues and the reference's own rounding of p + offset.
 // Every other query goes to the deferred list that the per-query kernel
 // finishes: short or overflowing lists, undecided sets or orders, tiles over
 // capacity, no previous smoothing length (first evaluation), and queries of
@@ -512,9 +514,9 @@ constexpr int kTileBox = 1024;
 template <int NR>
 struct TileSmem {
     static constexpr int LCAP = 24 * NR;  // per-query list capacity (>= 1.5 k)
-    // k <= 37: the k+1 smallest keys are kept in A registers per lane
-    static constexpr bool REG = NR <= 2;
-    static constexpr int A = NR == 1 ? 18 : 38;
+    // k <= 80: the k+1 smallest keys are kept in A registers per lane
+    static constexpr bool REG = NR <= 4;
+    static constexpr int A = NR == 1 ? 18 : NR == 2 ? 38 : 81;
     float2 rec[kTileCap];             // candidate positions relative to the group origin
     uint32_t code[kTileCap];          // (slot << kCodeShift) | image
     int4 rect[32];                    // per query: cell rectangle at the tile level
@@ -592,9 +594,12 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
             }
             BX0 = X0 >> sh; BX1 = X1 >> sh; BY0 = Y0 >> sh; BY1 = Y1 >> sh;
         }
-        // group origin: the first particle's FP64 position
+        // group origin: the first particle, as its FP64 position and as its
+        // float-pair record (relative to the grid origin)
         const double2 P = valid ? B.pos[q] : make_double2(0.0, 0.0);
         const double gx = __shfl_sync(FULL, P.x, 0), gy = __shfl_sync(FULL, P.y, 0);
+        const float ohx = __shfl_sync(FULL, pr.x, 0), olx = __shfl_sync(FULL, pr.z, 0);
+        const float ohy = __shfl_sync(FULL, pr.y, 0), oly = __shfl_sync(FULL, pr.w, 0);
         int total = 0;
         if (!defer_all) {
             const int shift = level - sh, Gl = 1 << shift;
@@ -681,13 +686,19 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
                             }
                             const int j = __shfl_sync(FULL, cbase, src) + t;
                             if (t < tot) {
-                                const double2 Q = B.pos[j];
-                                // the image's virtual position (q shifted by wx periods), then
-                                // relative to the group origin, rounded once to FP32
-                                const double qx = wx ? __dadd_rn(Q.x, (double)wx * Lx) : Q.x;
-                                const double qy = wy ? __dadd_rn(Q.y, (double)wy * Ly) : Q.y;
-                                sm.rec[total + t] = make_float2(__double2float_rn(__dsub_rn(qx, gx)),
-                                                                __double2float_rn(__dsub_rn(qy, gy)));
+                                if (img == 4) {
+                                    // relative to the group origin from the float pairs (FP32 only)
+                                    const float4 r = __ldg(&B.rec[j]);
+                                    sm.rec[total + t] = make_float2((r.x - ohx) + (r.z - olx), (r.y - ohy) + (r.w - oly));
+                                } else {
+                                    // an image: its virtual position (q shifted by wx periods) in
+                                    // FP64, relative to the group origin, rounded once to FP32
+                                    const double2 Q = B.pos[j];
+                                    const double qx = wx ? __dadd_rn(Q.x, (double)wx * Lx) : Q.x;
+                                    const double qy = wy ? __dadd_rn(Q.y, (double)wy * Ly) : Q.y;
+                                    sm.rec[total + t] = make_float2(__double2float_rn(__dsub_rn(qx, gx)),
+                                                                    __double2float_rn(__dsub_rn(qy, gy)));
+                                }
                                 sm.code[total + t] = ((uint32_t)j << kCodeShift) | img;
                                 if (img == 4 && j >= g0 && j < g0 + 32) sm.self[j - g0] = total + t;
                             }
@@ -705,17 +716,22 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
             __syncwarp();
             continue;
         }
-        // ---- each lane scans the tile for its own query
-        const float rqx = __double2float_rn(__dsub_rn(P.x, gx)), rqy = __double2float_rn(__dsub_rn(P.y, gy));
+        // ---- each lane scans the tile for its own query (its own record's
+        // relative coordinates, computed as the tile's unshifted records are)
+        const float rqx = (pr.x - ohx) + (pr.z - olx), rqy = (pr.y - ohy) + (pr.w - oly);
         const int myself = sm.self[lane];
         const float R2 = valid ? R * R : -1.f;
         const float qs = valid ? 8388608.f / R2 : 0.f;  // key units: R^2 / 2^23
         int cnt = 0;
         int t = 0;
+        const float4 *rec2 = reinterpret_cast<const float4 *>(sm.rec);  // two records per load
         for (; t + 4 <= total; t += 4) {
             float2 c[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) c[u] = sm.rec[t + u];
+            const float4 ab = rec2[t >> 1], cd = rec2[(t >> 1) + 1];
+            c[0] = make_float2(ab.x, ab.y);
+            c[1] = make_float2(ab.z, ab.w);
+            c[2] = make_float2(cd.x, cd.y);
+            c[3] = make_float2(cd.z, cd.w);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const float dx = c[u].x - rqx, dy = c[u].y - rqy;
@@ -747,7 +763,8 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
         const float ox = pxr - rqx, oy = pyr - rqy;      // group origin in grid coordinates
         const float Dx = fmaxf(fabsf((float)(BX0 << sh) * sx0 - ox), fabsf((float)((BX1 + 1) << sh) * sx0 - ox));
         const float Dy = fmaxf(fabsf((float)(BY0 << sh) * sy0 - oy), fabsf((float)((BY1 + 1) << sh) * sy0 - oy));
-        const float ea = kEpsRel * (R2 + 2.f * R * (Dx + Dy)) + 1.8e-15f * fmaxf(S.flmax, S.fmag) * R;
+        // (the last term also covers the float-pair residues of the records, 2^-48 |p - origin|)
+        const float ea = kEpsRel * (R2 + 2.f * R * (Dx + Dy)) + 2.3e-13f * fmaxf(S.flmax, S.fmag) * R;
         if (TS::REG) {
             // the A smallest keys, ascending, by a branch-free insertion chain
             // per list entry (registers only: no divergence, no smem latency chain)
