@@ -144,6 +144,9 @@ int sph_append(sph_handle *h, int64_t count, const double *x, const double *y, c
  * disks are painted in descending Z (the reference sorts by -Z), ties by
  * caller index, so the smallest Z ends on top. */
 int sph_set_draw_keys(sph_handle *h, const int64_t *z);
+/* gx.ParaRamp (gx/graphics.go:156-164) for every index 0..255 as NRGBA bytes
+ * (1024 bytes): the colour table the frames use. No device needed. */
+int sph_para_ramp(uint8_t *rgba);
 /* Renders the current state into rgba (width*height*4 bytes, NRGBA, row y =
  * Pos.Y*height from the top): black background, a disk of radius 4 pixels per
  * particle at (Pos.X*width, Pos.Y*height) with the reference's float32 pixel

@@ -88,6 +88,7 @@ def lib():
         L.orc_draw_order.argtypes = [C.c_int64, i64p, i64p]
         u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
         L.orc_render.argtypes = [C.c_int64, dp, dp, dp, C.c_double, i64p, C.c_int, C.c_int, u8p]
+        L.orc_para_ramp.argtypes = [C.c_int, u8p]
         for f in (L.orc_kernel_fpref, L.orc_kernel_dfpref):
             f.argtypes = [C.c_int]
             f.restype = C.c_double
@@ -210,6 +211,14 @@ def draw_order(z):
     order = np.empty(len(z), np.int64)
     lib().orc_draw_order(len(z), z, order)
     return order
+
+
+def para_ramp():
+    """gx.ParaRamp for every index: (256, 3) bytes."""
+    out = np.empty((256, 3), np.uint8)
+    for i in range(256):
+        lib().orc_para_ramp(i, out[i])
+    return out
 
 
 def render(x, y, rho, mass, order, width=1280, height=720):

@@ -924,6 +924,8 @@ static void para_ramp(int index, uint8_t *rgb) {
     rgb[0] = (uint8_t)r; rgb[1] = (uint8_t)g; rgb[2] = (uint8_t)b;
 }
 
+void orc_para_ramp(int index, uint8_t *rgb) { para_ramp(index, rgb); }
+
 /* sim/animator.go:55-103 CurrentFrame: black canvas, then for each particle in
  * `order` a disk of radius 4 (gx/graphics.go:90-107 DrawDisk, float32 pixel
  * test) coloured by ParaRamp(uint8(min(rho/(m*N*10)*256, 255))). x, y, rho in

@@ -24,8 +24,9 @@
  * sets the GPU path must reproduce bit for bit.
  *
  * Pinning: the Partition restatement is checked against the thirteen cases of
- * the reference's sim/partition_test.go and the sphere builder against the
- * containment property of sim/bounding-sphere_test.go. The reference has no
+ * the reference's sim/partition_test.go, the sphere builder against the
+ * containment property of sim/bounding-sphere_test.go, and the frame's colour
+ * ramp against the reference's own output image doc/customColorMaps.png. The reference has no
  * tests or vectors for kNN, density, force or the integrator and its Go
  * toolchain is not available, so those restatements are pinned only by
  * analytic known-answer tests and by the agreement of the two independent kNN
@@ -127,6 +128,7 @@ int orc_append(orc_sim *s, int n_new, const double *x, const double *y, const do
 /* Frames (sim/animator.go:55-103): draw order by the reference's QuickSort
  * on -Z (sim/heap.go:229-268), and the painted NRGBA canvas. */
 void orc_draw_order(int64_t n, const int64_t *z, int64_t *order);
+void orc_para_ramp(int index, uint8_t *rgb);  /* gx/graphics.go:156-164 */
 void orc_render(int64_t n, const double *x, const double *y, const double *rho, double mass,
                 const int64_t *order, int W, int H, uint8_t *rgba);
 

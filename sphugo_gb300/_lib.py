@@ -41,7 +41,7 @@ EXPORTS = [
     "sph_ic_stress", "sph_ic_ensemble", "sph_config_default", "sph_config_load",
     "sph_config_start_count", "sph_config_spawn", "sph_point_source_spawn",
     "sph_step_timed", "sph_step_profiled", "sph_kernels_per_step", "sph_set_search", "sph_search_stats",
-    "sph_probe_peaks", "sph_append", "sph_set_draw_keys", "sph_render",
+    "sph_probe_peaks", "sph_append", "sph_set_draw_keys", "sph_render", "sph_para_ramp",
     "sph_density_noalloc", "sph_autotune", "sph_save", "sph_load", "sph_selftest_division",
 ]
 NOALLOC_MAX_N = 8192
@@ -146,6 +146,7 @@ def load() -> C.CDLL:
     L.sph_append.argtypes = [vp, C.c_int64, dp, dp, dp, dp, dp, C.POINTER(C.c_int64)]
     L.sph_set_draw_keys.argtypes = [vp, C.POINTER(C.c_int64)]
     L.sph_render.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_uint8)]
+    L.sph_para_ramp.argtypes = [C.POINTER(C.c_uint8)]
     L.sph_search_stats.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.sph_probe_peaks.argtypes = [dp, dp, dp, dp]
     L.sph_autotune.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]

@@ -894,6 +894,12 @@ int32_t sph_kernels_per_step(sph_handle *h) {
     return h->kernels_per_step;
 }
 
+int sph_para_ramp(uint8_t *rgba) {
+    if (!rgba) return fail(SPH_ERR_ARG, "null buffer");
+    para_ramp_table(rgba);
+    return SPH_OK;
+}
+
 int sph_set_draw_keys(sph_handle *h, const int64_t *z) {
     if (!h) return fail(SPH_ERR_ARG, "null handle");
     Guard g(h);

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FIXTURES = sorted(glob.glob(os.path.join(HERE, "*.npz")))
+FIXTURES = sorted(glob.glob(os.path.join(HERE, "blast*.npz")))  # SPH runs (make_golden.py)
 STATE = ["x", "y", "vx", "vy", "u", "ax", "ay", "udot", "rho", "c", "h"]
 
 
@@ -49,3 +49,17 @@ def test_gpu_reproduces_fixture(gpu, path):
         assert np.array_equal(st[key], g["out_" + key]), key
     ids, dist, img = sim.neighbours()
     assert np.array_equal(ids, g["ids"]) and np.array_equal(img, g["img"]) and np.array_equal(dist, g["dist"])
+
+
+def test_colour_ramp_matches_the_reference_image(oracle, sphlib):
+    """ParaRamp of the frames against the colours in the reference's own
+    doc/customColorMaps.png (output of examples/color-ramp/color-ramp.go),
+    fixture made by tests/golden/make_ramp_golden.py."""
+    import ctypes as C
+
+    ref = np.load(os.path.join(HERE, "color_ramps_ref.npz"))["para"]
+    assert np.array_equal(oracle.para_ramp(), ref)
+    lut = np.zeros(1024, np.uint8)
+    assert sphlib.sph_para_ramp(lut.ctypes.data_as(C.POINTER(C.c_uint8))) == 0
+    lut = lut.reshape(256, 4)
+    assert np.array_equal(lut[:, :3], ref) and np.all(lut[:, 3] == 255)
