@@ -52,18 +52,19 @@ TOLERANCES = {"neighbour_sets": "bit-exact", "fp64": "bit-exact", "fp64_fast": 1
 #     distance and final square root of each kept neighbour,
 #     sim/nearest-neighbour.go:64-80): per neighbour d2 = ((p+o)-q)^2 7 ops,
 #     sqrt, div (q = d/h), kernel F (4 ops for q < 0.5, 3 + one division by 3
-#     otherwise), 1 add; per particle h = sqrt, rho (3 + div), c (3 + sqrt),
-#     cA (2 + div).
+#     otherwise), 1 add, and the force's dF(q) (4 ops for q < 0.5, 2
+#     otherwise; evaluated here and handed over); per particle h = sqrt,
+#     rho (3 + div), c (3 + sqrt), cA (2 + div).
 #   force (sim/sph.go:327-401 plus the leapfrog update :121-193):
-#     per neighbour dF (4 ops for q < 0.5, 2 otherwise), vAB 2, rAB 4, dot 3,
+#     per neighbour vAB 2, rAB 4, dot 3,
 #     (Pi + cA) + cB 2, x/y terms 2 x (2 + div + 1), du/dt term 2; per
 #     approaching pair (dot < 0) cAB, rhoAB, hAB 6, r2 3, mu 2 + div,
 #     Pi 5 + div; per particle the prefactor 3 + div, outputs 6, integrator 12.
 def algorithmic(k, div, sqrt, lo_frac, visc_frac):
     kern_f = lo_frac * 4 + (1 - lo_frac) * (3 + div)
     kern_df = lo_frac * 4 + (1 - lo_frac) * 2
-    dens = k * (7 + sqrt + div + kern_f + 1) + sqrt + (3 + div) + (3 + sqrt) + (2 + div)
-    force = k * (kern_df + 2 + 4 + 3 + 2 + 2 * (3 + div) + 2) + k * visc_frac * (6 + 3 + 2 + div + 5 + div) \
+    dens = k * (7 + sqrt + div + kern_f + kern_df + 1) + sqrt + (3 + div) + (3 + sqrt) + (2 + div)
+    force = k * (2 + 4 + 3 + 2 + 2 * (3 + div) + 2) + k * visc_frac * (6 + 3 + 2 + div + 5 + div) \
         + (3 + div) + 6 + 12
     return {
         "bin": {"bytes": 32 + 8},
