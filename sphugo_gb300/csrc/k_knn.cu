@@ -522,7 +522,7 @@ struct TileSmem {
     int4 rect[32];                    // per query: cell rectangle at the tile level
     int32_t rx0[kTileRows], rx1[kTileRows], rpre[kTileRows + 1];
     int32_t self[32];                 // tile slot of each query's own record
-    uint32_t list[LCAP][32];          // per-query keys, one column per query
+    uint32_t list[LCAP + 1][32];      // per-query keys, one column per query (+ a spare row)
 };
 
 __device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t q, int lane) {
@@ -732,30 +732,26 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
             c[1] = make_float2(ab.z, ab.w);
             c[2] = make_float2(cd.x, cd.y);
             c[3] = make_float2(cd.z, cd.w);
+            // branch-free: every record is written to the next free row (a
+            // spare row once the list is full) and counted only when it passes
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const float dx = c[u].x - rqx, dy = c[u].y - rqy;
                 const float d2 = __fmaf_rn(dx, dx, dy * dy);
-                if (d2 <= R2 && t + u != myself) {
-                    if (cnt < LCAP) {
-                        const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
-                        sm.list[cnt][lane] = (kq << 9) | (uint32_t)(t + u);
-                    }
-                    cnt++;
-                }
+                const bool pass = d2 <= R2 && t + u != myself;
+                const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
+                sm.list[min(cnt, LCAP)][lane] = (kq << 9) | (uint32_t)(t + u);
+                cnt += pass ? 1 : 0;
             }
         }
         for (; t < total; t++) {
             const float2 c = sm.rec[t];
             const float dx = c.x - rqx, dy = c.y - rqy;
             const float d2 = __fmaf_rn(dx, dx, dy * dy);
-            if (d2 <= R2 && t != myself) {
-                if (cnt < LCAP) {
-                    const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
-                    sm.list[cnt][lane] = (kq << 9) | (uint32_t)t;
-                }
-                cnt++;
-            }
+            const bool pass = d2 <= R2 && t != myself;
+            const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
+            sm.list[min(cnt, LCAP)][lane] = (kq << 9) | (uint32_t)t;
+            cnt += pass ? 1 : 0;
         }
         bool ok = valid && cnt >= k && cnt <= LCAP;
         // decisions in FP32 with the error bound eps
