@@ -285,7 +285,7 @@ void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) 
     launch_scan(c, L, h->T);
     launch_stable(c, L, h->T);
     mark(2);
-    launch_permute(c, L, h->A, h->B, h->T, pred, h->mode != MODE_FAST64);
+    launch_permute(c, L, h->A, h->B, h->T, pred, true);  // velocity records: every form's force reads them
     mark(3);
     launch_knn(c, L, h->B, h->D, h->T, h->mode, h->tune);
     mark(4);

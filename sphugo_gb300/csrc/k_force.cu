@@ -40,10 +40,10 @@ __device__ __forceinline__ void integrate_one(const SimDev &S, double2 &pos, dou
     if (pos.y > S.refl[3]) { pos.y = __dsub_rn(pos.y, __dsub_rn(pos.y, S.refl[3])); vel.y = -vel.y; }
 }
 
-// The fast-FP64 and mixed forms (the FP64 form is k_force_exact below).
+// The mixed form (the FP64 forms run k_force_fp64 below).
 template <int MODE>
 __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
-    static_assert(MODE != MODE_EXACT64, "the FP64 form runs k_force_exact");
+    static_assert(MODE == MODE_MIXED, "the FP64 forms run k_force_fp64");
     const int k = a.c.k;
     const PArrays &B = a.B;
     const Derived &D = a.D;
@@ -55,47 +55,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
         const double2 P = B.pos[q];
         const int32_t *nb = D.nbr + q * k;
         double axo, ayo, edot;
-        if (MODE == MODE_FAST64) {
-            const double4 di = D.der[q];
-            const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
-            const double inv_h = 1.0 / hi;
-            const double2 vpi = B.vp[q];
-            const double2 *dist = D.dist + q * k;
-            const double alpha = S.alpha, beta = S.beta, etasq = S.etasq;
-            double ax = 0.0, ay = 0.0, ed = 0.0;
-            for (int e = k - 1; e >= 0; e--) {
-                const uint32_t code = (uint32_t)nb[e];
-                const uint32_t j = code >> kCodeShift;
-                const double2 dd = dist[e];
-                const double qq = fmin(dd.x * inv_h, 1.0);
-                const double drk = kdf_fast(S.kernel, qq);
-                const double4 dj = D.der[j];
-                const double2 vpj = B.vp[j];
-                const double vabx = vpj.x - vpi.x, vaby = vpj.y - vpi.y;
-                double ox, oy;
-                img_shift(S, code & 15u, ox, oy);
-                const double2 Q = B.pos[j];
-                const double rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
-                const double raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
-                const double dot = vabx * rabx + vaby * raby;
-                double piab = 0.0;
-                if (dot < 0.0) {
-                    const double cab = 0.5 * (ci + dj.x);
-                    const double rhoab = 0.5 * (rhoi + dj.y);
-                    const double hab = 0.5 * (hi + dj.z);
-                    const double mu = dot * hab / (rabx * rabx + raby * raby + etasq);
-                    piab = mu * (beta * mu - alpha * cab) / rhoab;
-                }
-                const double w = (piab + ca + dj.w) * drk * dd.y;
-                ax += rabx * w;
-                ay += raby * w;
-                ed += dot * drk;
-            }
-            const double f = S.mass * S.dfpref * (inv_h * inv_h * inv_h);
-            axo = ax * f + S.accel[0];
-            ayo = ay * f + S.accel[1];
-            edot = ca * ed * S.mass;
-        } else {
+        {
             const float4 di = D.derf[q];
             const double hi = D.h[q];
             const double ca = D.c[q] * D.c[q] / (S.gamma * D.rho[q]);
@@ -210,7 +170,9 @@ __device__ __forceinline__ void pair_geom(const SimDev &S, const PArrays &B, uin
     dot = __dadd_rn(__dmul_rn(vabx, rabx), __dmul_rn(vaby, raby));
 }
 
-__global__ void __launch_bounds__(kForceWarps * 32) k_force_exact(ForceArgs a) {
+template <int MODE>
+__global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
+    static_assert(MODE == MODE_EXACT64 || MODE == MODE_FAST64, "FP64 forms only");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int k = a.c.k;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -314,14 +276,20 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_exact(ForceArgs a) {
             double rabx, raby, dot;
             pair_geom(Sp, B, code, Pp, vpp, rabx, raby, dot);
             const double4 dj = D.der[code >> kCodeShift];
-            const double cab = __dmul_rn(0.5, __dadd_rn(dp.x, dj.x));
-            const double rhoab = __dmul_rn(0.5, __dadd_rn(dp.y, dj.y));
-            const double hab = __dmul_rn(0.5, __dadd_rn(dp.z, dj.z));
-            const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
-            const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, Sp.etasq));
-            spi[e * 32 + p] = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-Sp.alpha, cab), mu),
-                                                  __dmul_rn(__dmul_rn(Sp.beta, mu), mu)),
-                                        rhoab);
+            if (MODE == MODE_EXACT64) {
+                const double cab = __dmul_rn(0.5, __dadd_rn(dp.x, dj.x));
+                const double rhoab = __dmul_rn(0.5, __dadd_rn(dp.y, dj.y));
+                const double hab = __dmul_rn(0.5, __dadd_rn(dp.z, dj.z));
+                const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
+                const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, Sp.etasq));
+                spi[e * 32 + p] = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-Sp.alpha, cab), mu),
+                                                      __dmul_rn(__dmul_rn(Sp.beta, mu), mu)),
+                                            rhoab);
+            } else {
+                const double cab = 0.5 * (dp.x + dj.x), rhoab = 0.5 * (dp.y + dj.y), hab = 0.5 * (dp.z + dj.z);
+                const double mu = dot * hab / (rabx * rabx + raby * raby + Sp.etasq);
+                spi[e * 32 + p] = mu * (Sp.beta * mu - Sp.alpha * cab) / rhoab;
+            }
         }
         __syncwarp();
         // ---- 3. the reference's ordered sums
@@ -331,26 +299,52 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_exact(ForceArgs a) {
             (void)rhoi;
             const double2 *dist = D.dist + q * k;
             double ax = 0.0, ay = 0.0, ed = 0.0;
-            for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
-                const uint32_t code = (uint32_t)nb[e];
-                const double d = dist[e].x;
-                const double drk = dist[e].y;  // dF(NNDists[i]/maxR), evaluated by the density pass
-                double rabx, raby, dot;
-                pair_geom(S, B, code, P, vpi, rabx, raby, dot);
-                const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;
-                const double piab = visc ? spi[e * 32 + lane] : 0.0;
-                const double cb = D.der[code >> kCodeShift].w;
-                const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
-                // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
-                const double yd = __drcp_rn(d);
-                ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
-                ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
-                ed = __dadd_rn(ed, __dmul_rn(dot, drk));
+            double axo, ayo, edot;
+            if (MODE == MODE_EXACT64) {
+                for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
+                    const uint32_t code = (uint32_t)nb[e];
+                    const double d = dist[e].x;
+                    const double drk = dist[e].y;  // dF(NNDists[i]/maxR), evaluated by the density pass
+                    double rabx, raby, dot;
+                    pair_geom(S, B, code, P, vpi, rabx, raby, dot);
+                    const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;
+                    const double piab = visc ? spi[e * 32 + lane] : 0.0;
+                    const double cb = D.der[code >> kCodeShift].w;
+                    const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
+                    // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
+                    const double yd = __drcp_rn(d);
+                    ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
+                    ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
+                    ed = __dadd_rn(ed, __dmul_rn(dot, drk));
+                }
+                const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
+                axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
+                ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
+                edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
+            } else {
+                // the fast form keeps (dF, dF / NNDists) per neighbour
+                for (int e = k - 1; e >= 0; e--) {
+                    const uint32_t code = (uint32_t)nb[e];
+                    const double2 dd = dist[e];
+                    const uint32_t j = code >> kCodeShift;
+                    const double2 vpj = B.vp[j], Q = B.pos[j];
+                    double ox = 0.0, oy = 0.0;
+                    if ((code & 15u) != 4u) img_shift(S, code & 15u, ox, oy);
+                    const double rabx = (Q.x - ox) - P.x, raby = (Q.y - oy) - P.y;
+                    const double dot = (vpj.x - vpi.x) * rabx + (vpj.y - vpi.y) * raby;
+                    const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;
+                    const double piab = visc ? spi[e * 32 + lane] : 0.0;
+                    const double w = (piab + ca + D.der[j].w) * dd.y;
+                    ax += rabx * w;
+                    ay += raby * w;
+                    ed += dot * dd.x;
+                }
+                const double inv_h = 1.0 / hi;
+                const double f = S.mass * S.dfpref * (inv_h * inv_h * inv_h);
+                axo = ax * f + S.accel[0];
+                ayo = ay * f + S.accel[1];
+                edot = ca * ed * S.mass;
             }
-            const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
-            const double axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
-            const double ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
-            const double edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
             if (!isfinite(axo) || !isfinite(ayo) || !isfinite(edot)) fl |= FLAG_Q_RANGE;
             double2 pos = P, vel = B.vel[q];
             double u = B.u[q];
@@ -377,10 +371,11 @@ static int g_force_exact_blocks[129];  // resident blocks per SM by k (filled be
 // Sets the shared-memory limit of the FP64 force kernel and records its
 // occupancy for k; must run before any stream capture.
 void force_init_attrs(int k) {
-    cudaFuncSetAttribute(k_force_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_exact_smem(128));
+    cudaFuncSetAttribute(k_force_fp64<MODE_EXACT64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_exact_smem(128));
+    cudaFuncSetAttribute(k_force_fp64<MODE_FAST64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)force_exact_smem(128));
     if (k >= 1 && k <= 128 && !g_force_exact_blocks[k]) {
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_exact, kForceWarps * 32, force_exact_smem(k));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_fp64<MODE_EXACT64>, kForceWarps * 32, force_exact_smem(k));
         g_force_exact_blocks[k] = std::max(nb, 1);
     }
 }
@@ -397,13 +392,14 @@ void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays
     int64_t need = (c.n + block - 1) / block;
     int grid = (int)(need < (int64_t)L.sms * 16 ? need : (int64_t)L.sms * 16);
     if (grid < 1) grid = 1;
-    if (mode == MODE_EXACT64) {
+    if (mode == MODE_EXACT64 || mode == MODE_FAST64) {
         const int64_t tiles = (c.n + 31) / 32;
         const int64_t eneed = (tiles + kForceWarps - 1) / kForceWarps;
         const int nb = c.k >= 1 && c.k <= 128 ? std::max(g_force_exact_blocks[c.k], 1) : 1;
         const int eg = (int)std::max<int64_t>(1, std::min<int64_t>(eneed, (int64_t)L.sms * nb));
-        k_force_exact<<<eg, kForceWarps * 32, force_exact_smem(c.k), L.stream>>>(a);
-    } else if (mode == MODE_FAST64) k_force<MODE_FAST64><<<grid, block, 0, L.stream>>>(a);
+        if (mode == MODE_EXACT64) k_force_fp64<MODE_EXACT64><<<eg, kForceWarps * 32, force_exact_smem(c.k), L.stream>>>(a);
+        else k_force_fp64<MODE_FAST64><<<eg, kForceWarps * 32, force_exact_smem(c.k), L.stream>>>(a);
+    }
     else k_force<MODE_MIXED><<<grid, block, 0, L.stream>>>(a);
 }
 

@@ -169,8 +169,10 @@ def normalised_errors(g_state, g_der, o_state, anorm, unorm):
 
 
 def test_fast64_within_1e12(gpu, oracle):
-    conf, arrs = blast(3000, seed=5, precision="Fast")
-    g, o = pair(oracle, conf, arrs)
+    conf, (x, y, _, _, u) = blast(3000, seed=5, precision="Fast")
+    rng = np.random.default_rng(5)
+    vx, vy = rng.normal(0, 0.3, x.size), rng.normal(0, 0.3, x.size)  # viscosity on about half the pairs
+    g, o = pair(oracle, conf, (x, y, vx, vy, u))
     g.Step(1)
     o.step(1)
     gi, gd, gm = g.neighbours()
