@@ -29,6 +29,7 @@
 #include "physics.cuh"
 
 #include <algorithm>
+#include <cstddef>
 
 namespace sphgpu {
 
@@ -522,8 +523,12 @@ struct TileSmem {
     int4 rect[32];                    // per query: cell rectangle at the tile level
     int32_t rx0[kTileRows], rx1[kTileRows], rpre[kTileRows + 1];
     int32_t self[32];                 // tile slot of each query's own record
-    uint32_t list[LCAP + 1][32];      // per-query keys, one column per query (+ a spare row)
+    alignas(16) uint32_t list[LCAP + 1][32];  // per-query keys, one column per query (+ a spare row)
 };
+static_assert(offsetof(TileSmem<1>, list) % 16 == 0 && offsetof(TileSmem<2>, list) % 16 == 0 &&
+                  offsetof(TileSmem<4>, list) % 16 == 0 && offsetof(TileSmem<8>, list) % 16 == 0 &&
+                  sizeof(TileSmem<2>) % 16 == 0 && offsetof(TileSmem<2>, rect) % 16 == 0,
+              "tile shared-memory members must keep their alignment");
 
 __device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t q, int lane) {
     const uint32_t bal = __ballot_sync(0xffffffffu, mine);
@@ -944,17 +949,40 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
             const double inv_h = 1.0 / h;
-            double acc = 0.0;
+            // q and 1/NNDists first; then the kernel sums and dF in branch-split
+            // loops (q grows with e), leaving (dF, dF / NNDists) for the force
+            int s_lo = 0;
             for (int e = k - 1; e >= 0; e--) {
                 const double d2 = e == k - 1 ? dk2 : nbr_d2(S, B, P, (uint32_t)nb[e]);
                 const double y = rsqrt(d2);
-                const double d = d2 * y;
-                const double x = fmin(d * inv_h, 1.0);
-                if (!(x >= 0.0)) fl |= FLAG_Q_RANGE;
-                acc += kf_fast(S.kernel, x);
-                dist[e] = make_double2(d, y);
+                const double x = fmin(d2 * y * inv_h, 1.0);
+                s_lo += x < 0.5;
+                dist[e] = make_double2(x, y);
+            }
+            double acc = 0.0;
+            if (S.kernel == SPH_KERNEL_WENDLAND) {
+                for (int e = k - 1; e >= 0; e--) {
+                    const double2 xy = dist[e];
+                    acc += kf_fast(SPH_KERNEL_WENDLAND, xy.x);
+                    const double drk = kdf_fast(SPH_KERNEL_WENDLAND, xy.x);
+                    dist[e] = make_double2(drk, drk * xy.y);
+                }
+            } else {
+                for (int e = k - 1; e >= s_lo; e--) {
+                    const double2 xy = dist[e];
+                    const double a1 = 1.0 - xy.x, a2 = a1 * a1;
+                    acc += a2 * a1 * (1.0 / 3.0);
+                    dist[e] = make_double2(-a2, -a2 * xy.y);
+                }
+                for (int e = s_lo - 1; e >= 0; e--) {
+                    const double2 xy = dist[e];
+                    acc += (xy.x - 1.0) * xy.x * xy.x + (1.0 / 6.0);
+                    const double drk = (3.0 * xy.x - 2.0) * xy.x;
+                    dist[e] = make_double2(drk, drk * xy.y);
+                }
             }
             rho = S.fpref * S.mass * acc * (inv_h * inv_h);
+            if (!(rho >= 0.0 && rho < 1.0e308)) fl |= FLAG_Q_RANGE;
             cs = sqrt(gamma * (gamma - 1.0) * up);
             cterm = cs * cs / (gamma * rho);
         } else {
