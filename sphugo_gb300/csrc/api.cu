@@ -657,7 +657,37 @@ int sph_append(sph_handle *h, int64_t count, const double *x, const double *y, c
         const Derived oldD = h->D;
         const Tables oldT = h->T;
         double *old_io = h->d_io;
-        if (alloc_particles(h, cap)) return fail(SPH_ERR_NOMEM, "cannot grow the particle arrays");
+        const int64_t old_cap = h->cap_n;
+        const size_t old_io_doubles = h->io_doubles;
+        if (alloc_particles(h, cap)) {
+            // release whatever the failed attempt got and keep the old arrays
+            const PArrays newA = h->A, newB = h->B;
+            const Derived newD = h->D;
+            const Tables newT = h->T;
+            double *new_io = h->d_io;
+            auto drop = [&](void *nw, void *old) {
+                if (nw && nw != old) dfree(h, nw);
+            };
+            drop(newA.pos, oldA.pos); drop(newA.vel, oldA.vel); drop(newA.vp, oldA.vp); drop(newA.acc, oldA.acc);
+            drop(newA.u, oldA.u); drop(newA.up, oldA.up); drop(newA.udot, oldA.udot); drop(newA.id, oldA.id);
+            drop(newA.hprev, oldA.hprev); drop(newA.rec, oldA.rec); drop(newA.vrec, oldA.vrec);
+            drop(newB.pos, oldB.pos); drop(newB.vel, oldB.vel); drop(newB.vp, oldB.vp); drop(newB.acc, oldB.acc);
+            drop(newB.u, oldB.u); drop(newB.up, oldB.up); drop(newB.udot, oldB.udot); drop(newB.id, oldB.id);
+            drop(newB.hprev, oldB.hprev); drop(newB.rec, oldB.rec); drop(newB.vrec, oldB.vrec);
+            drop(newD.rho, oldD.rho); drop(newD.c, oldD.c); drop(newD.h, oldD.h); drop(newD.nbr, oldD.nbr);
+            drop(newD.defer, oldD.defer); drop(newD.der, oldD.der); drop(newD.derf, oldD.derf);
+            drop(newD.dist, oldD.dist); drop(newD.d2f, oldD.d2f);
+            drop(newT.key, oldT.key); drop(newT.rank, oldT.rank); drop(newT.tmp, oldT.tmp);
+            drop(new_io, old_io);
+            h->A = oldA;
+            h->B = oldB;
+            h->D = oldD;
+            h->T = oldT;
+            h->d_io = old_io;
+            h->cap_n = old_cap;
+            h->io_doubles = old_io_doubles;
+            return fail(SPH_ERR_NOMEM, "cannot grow the particle arrays");
+        }
         h->D.ndefer = oldD.ndefer;
         h->T.count = oldT.count;
         h->T.start = oldT.start;
@@ -1174,6 +1204,14 @@ int sph_load(sph_handle *h, const char *path) {
     if (hd.n != h->n || hd.nsims != h->nsims || hd.k != h->k || hd.mode != (uint32_t)h->mode ||
         hd.params_hash != params_hash(h))
         return fail(SPH_ERR_ARG, "checkpoint was written by a handle with other parameters or sizes");
+    // read the whole payload first: a truncated file leaves the handle untouched
+    const std::vector<ArrayRef> arrays = state_arrays(h);
+    std::vector<std::vector<char>> bufs(arrays.size());
+    for (size_t i = 0; i < arrays.size(); i++) {
+        bufs[i].resize(arrays[i].bytes);
+        f.read(bufs[i].data(), (std::streamsize)arrays[i].bytes);
+        if (!f) return fail(SPH_ERR_ARG, "truncated checkpoint");
+    }
     int rc;
     if (hd.level_delta != h->level_delta && (rc = apply_levels(h, hd.level_delta))) return rc;
     if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow || hd.tile != h->tune.tile) {
@@ -1182,14 +1220,9 @@ int sph_load(sph_handle *h, const char *path) {
         h->tune.tile = hd.tile;
         destroy_graphs(h);
     }
-    std::vector<char> buf;
-    for (const ArrayRef &a : state_arrays(h)) {
-        buf.resize(a.bytes);
-        f.read(buf.data(), (std::streamsize)a.bytes);
-        if (!f) return fail(SPH_ERR_ARG, "truncated checkpoint");
-        CUDA_TRY(cudaMemcpyAsync(a.dev, buf.data(), a.bytes, cudaMemcpyHostToDevice, h->stream));
-        CUDA_TRY(cudaStreamSynchronize(h->stream));
-    }
+    for (size_t i = 0; i < arrays.size(); i++)
+        CUDA_TRY(cudaMemcpyAsync(arrays[i].dev, bufs[i].data(), arrays[i].bytes, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->step = hd.step;
     h->uploaded = true;
     h->evaluated = false;

@@ -156,3 +156,20 @@ def test_group_tiles_cover_ensemble_boundaries_and_images(gpu):
         assert np.array_equal(s1[key], s2[key]), key
     q, d = e1.search_stats()
     assert d < q
+
+
+def test_truncated_checkpoint_leaves_the_state(gpu, tmp_path):
+    a = _sim(4000)
+    a.Step(2)
+    a.Save(tmp_path / "s.ck")
+    data = (tmp_path / "s.ck").read_bytes()
+    (tmp_path / "t.ck").write_bytes(data[: len(data) // 2])
+    b = _sim(4000)
+    b.Step(1)
+    before = b.state()
+    with pytest.raises(L.SphError):
+        b.Load(tmp_path / "t.ck")
+    after = b.state()
+    assert b.CurrentStep == 1
+    for key in before:
+        assert np.array_equal(before[key], after[key]), key
