@@ -194,6 +194,16 @@ def ncu_traffic(kernel, form, n):
     return ent.get("dram_bytes_per_launch") if ent else None
 
 
+def ncu_field(stage, form, n, field):
+    """Another figure of the committed ncu summary for a stage (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            ent = json.load(f).get(f"{stage}/{form.lower()}/{n}")
+    except (OSError, ValueError):
+        return None
+    return ent.get(field) if ent else None
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -398,6 +408,12 @@ def run_ours(args, dist):
             entry.update(bound="hbm", unit="GB/s", achieved=b / (t * 1e-3) / 1e9, peak=hbm_peak)
         if entry.get("peak"):
             entry["frac"] = entry["achieved"] / entry["peak"]
+        if st == "knn":
+            # no HBM or FP roofline binds the search: it is issue- and latency-bound
+            entry["binding"] = "instruction issue / shared-memory latency"
+            issue = ncu_field("knn", form, n, "issue_active_frac")
+            if issue is not None:
+                entry["ncu_issue_active_frac"] = issue
         roof[st] = entry
     dom = max(stages, key=stages.get)
     d = roof[dom]
