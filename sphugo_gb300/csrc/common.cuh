@@ -63,6 +63,8 @@ struct SimDev {
     float fimg_h[2], fimg_l[2]; // image shifts as float pairs (hi, lo)
     float flmax;           // max(L)
     float fmag;            // bound on |p + offset| of any particle image (the reference rounds it)
+    // FP32 copies of the constants the mixed form's sums use
+    float falpha, fbeta, fetasq, fgamma, fgg1, ffm, fdfm, fmass;
     unsigned long long bbox[4]; // open axes: ordered-key min x, max x, min y, max y
 };
 
@@ -162,6 +164,14 @@ __host__ __device__ inline void simdev_floats(SimDev &S) {
         mag = m > mag ? m : mag;
     }
     S.fmag = (float)mag;
+    S.falpha = (float)S.alpha;
+    S.fbeta = (float)S.beta;
+    S.fetasq = (float)S.etasq;
+    S.fgamma = (float)S.gamma;
+    S.fgg1 = (float)(S.gamma * (S.gamma - 1.0));
+    S.ffm = (float)(S.fpref * S.mass);
+    S.fdfm = (float)(S.mass * S.dfpref);
+    S.fmass = (float)S.mass;
 }
 
 // order-preserving 64-bit key of a double (for atomic min/max)

@@ -56,18 +56,15 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
         const int32_t *nb = D.nbr + q * k;
         double axo, ayo, edot;
         {
+            // FP32 throughout the sums and prefactors (no FP64 work per particle
+            // before the integrator)
             const float4 di = D.derf[q];
-            const double hi = D.h[q];
-            const double ca = D.c[q] * D.c[q] / (S.gamma * D.rho[q]);
             const float ci = di.x, rhoi = di.y, hif = di.z, caf = di.w;
             const float inv_hf = 1.f / hif;
             const float4 pr = B.rec[q];
             const float4 vi = B.vrec[q];
-            const float alpha = (float)S.alpha, beta = (float)S.beta, etasq = (float)S.etasq;
-            const float dXh = __double2float_rn(S.dimg[0]);
-            const float dXl = __double2float_rn(S.dimg[0] - (double)dXh);
-            const float dYh = __double2float_rn(S.dimg[1]);
-            const float dYl = __double2float_rn(S.dimg[1] - (double)dYh);
+            const float alpha = S.falpha, beta = S.fbeta, etasq = S.fetasq;
+            const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
             KahanF ax, ay, ed;
             for (int e = k - 1; e >= 0; e--) {
                 const uint32_t code = (uint32_t)nb[e];
@@ -77,9 +74,9 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                 const float4 r = __ldg(&B.rec[j]);
                 // r_AB = (q - offset) - p from float pairs (see the kNN kernel)
                 const float rabx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
-                                   (r.z - (pr.z + (float)ia * dXl));
+                                   (r.z - (pr.z + (ia > 0 ? dXl : ia < 0 ? -dXl : 0.f)));
                 const float raby = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
-                                   (r.w - (pr.w + (float)ib * dYl));
+                                   (r.w - (pr.w + (ib > 0 ? dYl : ib < 0 ? -dYl : 0.f)));
                 const float d2 = __fmaf_rn(rabx, rabx, raby * raby);
                 const float invd = rsqrtf(d2);
                 const float qq = fminf(d2 * invd * inv_hf, 1.f);
@@ -102,10 +99,10 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                 ay.add(raby * w);
                 ed.add(dot * drk);
             }
-            const double f = S.mass * S.dfpref / (hi * hi * hi);
-            axo = ax.value() * f + S.accel[0];
-            ayo = ay.value() * f + S.accel[1];
-            edot = ca * ed.value() * S.mass;
+            const float ff = S.fdfm * (inv_hf * inv_hf * inv_hf);
+            axo = (double)(ax.value_f() * ff) + S.accel[0];
+            ayo = (double)(ay.value_f() * ff) + S.accel[1];
+            edot = (double)(caf * ed.value_f() * S.fmass);
         }
         if (!isfinite(axo) || !isfinite(ayo) || !isfinite(edot)) fl |= FLAG_Q_RANGE;
         double2 pos = P, vel = B.vel[q];
@@ -214,9 +211,9 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                     const int ia = (int)((code & 15u) / 3u) - 1, ib = (int)((code & 15u) % 3u) - 1;
                     const float4 r = B.rec[j], vj = B.vrec[j];
                     const float rx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
-                                     (r.z - (pr.z + (float)ia * dXl));
+                                     (r.z - (pr.z + (ia > 0 ? dXl : ia < 0 ? -dXl : 0.f)));
                     const float ry = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
-                                     (r.w - (pr.w + (float)ib * dYl));
+                                     (r.w - (pr.w + (ib > 0 ? dYl : ib < 0 ? -dYl : 0.f)));
                     const float vx = (vj.x - vi.x) + (vj.z - vi.z), vy = (vj.y - vi.y) + (vj.w - vi.w);
                     const float px = vx * rx, py = vy * ry;
                     const float dotf = px + py;

@@ -530,6 +530,14 @@ static_assert(offsetof(TileSmem<1>, list) % 16 == 0 && offsetof(TileSmem<2>, lis
                   sizeof(TileSmem<2>) % 16 == 0 && offsetof(TileSmem<2>, rect) % 16 == 0,
               "tile shared-memory members must keep their alignment");
 
+// d2 in units of R^2 / 2^23 rounded to the nearest integer, clamped to 23
+// bits, without a conversion instruction: for 0 <= d2 qs < 2^23 the FMA
+// d2 qs + 2^23 lands in [2^23, 2^24), where the float's mantissa is the
+// integer itself.
+__device__ __forceinline__ uint32_t key23(float d2, float qs) {
+    return min(__float_as_uint(__fmaf_rn(d2, qs, 8388608.f)) - 0x4B000000u, 8388607u);
+}
+
 __device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t q, int lane) {
     const uint32_t bal = __ballot_sync(0xffffffffu, mine);
     if (!bal) return;
@@ -744,7 +752,7 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
                 const float dx = c[u].x - rqx, dy = c[u].y - rqy;
                 const float d2 = __fmaf_rn(dx, dx, dy * dy);
                 const bool pass = d2 <= R2 && t + u != myself;
-                const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
+                const uint32_t kq = key23(d2, qs);
                 sm.list[min(cnt, LCAP)][lane] = (kq << 9) | (uint32_t)(t + u);
                 cnt += pass ? 1 : 0;
             }
@@ -754,7 +762,7 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
             const float dx = c.x - rqx, dy = c.y - rqy;
             const float d2 = __fmaf_rn(dx, dx, dy * dy);
             const bool pass = d2 <= R2 && t != myself;
-            const uint32_t kq = min(__float2uint_rz(d2 * qs), 8388607u);
+            const uint32_t kq = key23(d2, qs);
             sm.list[min(cnt, LCAP)][lane] = (kq << 9) | (uint32_t)t;
             cnt += pass ? 1 : 0;
         }
@@ -990,24 +998,28 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             const double dk2 = nbr_d2(S, B, B.pos[q], (uint32_t)a.D.nbr[q * k + k - 1]);
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
             h = __dsqrt_rn(dk2);
-            const float inv_hf = 1.f / __double2float_rn(h);
+            // everything after h in FP32 (prefactors from FP32 copies)
+            const float hf = __double2float_rn(h);
+            const float inv_hf = 1.f / hf;
             const float *d2f = a.D.d2f + q * k;
             KahanF acc;
             for (int e = k - 1; e >= 0; e--) {
                 const float x = fminf(sqrtf(d2f[e]) * inv_hf, 1.f);
                 acc.add(kf_f32(S.kernel, x));
             }
-            rho = (S.fpref * S.mass / (h * h)) * acc.value();
-            cs = sqrt(gamma * (gamma - 1.0) * up);
-            cterm = cs * cs / (gamma * rho);
+            const float rhof = S.ffm * (inv_hf * inv_hf) * acc.value_f();
+            const float csf = sqrtf(S.fgg1 * __double2float_rn(up));
+            const float ctf = csf * csf / (S.fgamma * rhof);
+            a.D.rho[q] = rhof;
+            a.D.c[q] = csf;
+            a.D.h[q] = h;
+            a.D.derf[q] = make_float4(csf, rhof, hf, ctf);
+            continue;
         }
         a.D.rho[q] = rho;
         a.D.c[q] = cs;
         a.D.h[q] = h;
-        if (MODE == MODE_MIXED)
-            a.D.derf[q] = make_float4((float)cs, (float)rho, (float)h, (float)cterm);
-        else
-            a.D.der[q] = make_double4(cs, rho, h, cterm);
+        a.D.der[q] = make_double4(cs, rho, h, cterm);
     }
     if (fl) atomicOr(a.c.flags, fl);
 }

@@ -112,6 +112,7 @@ struct KahanF {
         s = t;
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ float value_f() const { return s - c; }
 };
 
 // The reference's squared distance of the image-shifted query to a
