@@ -809,19 +809,33 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
             ok = ok && (cnt == k || nxt - tau > 2.f * (kEpsRel * nxt + ea));
             if (MODE == MODE_MIXED) ok = ok && (k == 1 || tau - prv > 2.f * et);
             else ok = ok && order_ok;
-            if (ok) {
+            if (ok && MODE == MODE_MIXED) {
+                // the mixed form needs the set, with the farthest last (it fixes h):
+                // the entries up to the k-th key in tile (cell) order, which keeps
+                // the force pass's gathers close in memory
+                uint32_t kth = 0;
+#pragma unroll
+                for (int i = 0; i < A; i++)
+                    if (i == k - 1) kth = arr[i];
+                int32_t *out = a.D.nbr + q * k;
+                float *o2 = a.D.d2f + q * k;
+                int o = 0;
+                for (int e = 0; e < cnt; e++) {
+                    const uint32_t v = sm.list[e][lane];
+                    if (v <= kth) {
+                        const uint32_t slot = v & 511u;
+                        const float2 c = sm.rec[slot];
+                        const float dx = c.x - rqx, dy = c.y - rqy;
+                        const int at = v == kth ? k - 1 : o++;
+                        out[at] = (int32_t)sm.code[slot];
+                        o2[at] = __fmaf_rn(dx, dx, dy * dy);
+                    }
+                }
+            } else if (ok) {
                 int32_t *out = a.D.nbr + q * k;
 #pragma unroll
                 for (int i = 0; i < A; i++) {
-                    if (i < k) {
-                        const uint32_t slot = arr[i] & 511u;
-                        out[i] = (int32_t)sm.code[slot];
-                        if (MODE == MODE_MIXED) {
-                            const float2 c = sm.rec[slot];
-                            const float dx = c.x - rqx, dy = c.y - rqy;
-                            a.D.d2f[q * k + i] = __fmaf_rn(dx, dx, dy * dy);
-                        }
-                    }
+                    if (i < k) out[i] = (int32_t)sm.code[arr[i] & 511u];
                 }
             }
         } else if (ok) {
