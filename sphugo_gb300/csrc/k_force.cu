@@ -66,8 +66,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
             const float alpha = S.falpha, beta = S.fbeta, etasq = S.fetasq;
             const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
             KahanF ax, ay, ed;
-            for (int e = k - 1; e >= 0; e--) {
-                const uint32_t code = (uint32_t)nb[e];
+            auto pair = [&](uint32_t code) {
                 const uint32_t j = code >> kCodeShift;
                 const uint32_t img = code & 15u;
                 const int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
@@ -98,6 +97,19 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                 ax.add(rabx * w);
                 ay.add(raby * w);
                 ed.add(dot * drk);
+            };
+            // neighbours farthest first; four codes per load when k allows
+            if ((k & 3) == 0) {
+                const int4 *nb4 = reinterpret_cast<const int4 *>(nb);
+                for (int b = (k >> 2) - 1; b >= 0; b--) {
+                    const int4 c4 = nb4[b];
+                    pair((uint32_t)c4.w);
+                    pair((uint32_t)c4.z);
+                    pair((uint32_t)c4.y);
+                    pair((uint32_t)c4.x);
+                }
+            } else {
+                for (int e = k - 1; e >= 0; e--) pair((uint32_t)nb[e]);
             }
             const float ff = S.fdfm * (inv_hf * inv_hf * inv_hf);
             axo = (double)(ax.value_f() * ff) + S.accel[0];

@@ -1017,9 +1017,18 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             const float inv_hf = 1.f / hf;
             const float *d2f = a.D.d2f + q * k;
             KahanF acc;
-            for (int e = k - 1; e >= 0; e--) {
-                const float x = fminf(sqrtf(d2f[e]) * inv_hf, 1.f);
-                acc.add(kf_f32(S.kernel, x));
+            auto term = [&](float v) { acc.add(kf_f32(S.kernel, fminf(sqrtf(v) * inv_hf, 1.f))); };
+            if ((k & 3) == 0) {  // farthest first, four values per load
+                const float4 *d4 = reinterpret_cast<const float4 *>(d2f);
+                for (int b = (k >> 2) - 1; b >= 0; b--) {
+                    const float4 v = d4[b];
+                    term(v.w);
+                    term(v.z);
+                    term(v.y);
+                    term(v.x);
+                }
+            } else {
+                for (int e = k - 1; e >= 0; e--) term(d2f[e]);
             }
             const float rhof = S.ffm * (inv_hf * inv_hf) * acc.value_f();
             const float csf = sqrtf(S.fgg1 * __double2float_rn(up));
