@@ -98,19 +98,7 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                 ay.add(raby * w);
                 ed.add(dot * drk);
             };
-            // neighbours farthest first; four codes per load when k allows
-            if ((k & 3) == 0) {
-                const int4 *nb4 = reinterpret_cast<const int4 *>(nb);
-                for (int b = (k >> 2) - 1; b >= 0; b--) {
-                    const int4 c4 = nb4[b];
-                    pair((uint32_t)c4.w);
-                    pair((uint32_t)c4.z);
-                    pair((uint32_t)c4.y);
-                    pair((uint32_t)c4.x);
-                }
-            } else {
-                for (int e = k - 1; e >= 0; e--) pair((uint32_t)nb[e]);
-            }
+            for_each_nbr_desc(nb, k, [&](int, uint32_t code) { pair(code); });
             const float ff = S.fdfm * (inv_hf * inv_hf * inv_hf);
             axo = (double)(ax.value_f() * ff) + S.accel[0];
             ayo = (double)(ay.value_f() * ff) + S.accel[1];
@@ -214,11 +202,9 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
             const float4 pr = B.rec[q], vi = B.vrec[q];
             const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
             const float lbig = 2.f * fmaxf(S.flmax, S.fmag);
-            for (int wd = 0; wd < nw; wd++) {
-                uint32_t m = 0;
-                const int e1 = min(k, (wd + 1) * 32);
-                for (int e = wd * 32; e < e1; e++) {
-                    const uint32_t code = (uint32_t)nb[e];
+            uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;  // approach bits of entries 0-31, 32-63, ...
+            for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {
+                {
                     const uint32_t j = code >> kCodeShift;
                     const int ia = (int)((code & 15u) / 3u) - 1, ib = (int)((code & 15u) % 3u) - 1;
                     const float4 r = B.rec[j], vj = B.vrec[j];
@@ -242,10 +228,22 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                         pair_geom(S, B, code, P, vpi, rabx, raby, dot);
                         approach = dot < 0.0;
                     }
-                    if (approach) m |= 1u << (e & 31);
+                    if (approach) {
+                        const uint32_t bit = 1u << (e & 31);
+                        if (e < 32) m0 |= bit;
+                        else if (e < 64) m1 |= bit;
+                        else if (e < 96) m2 |= bit;
+                        else m3 |= bit;
+                    }
                 }
-                smask[wd * 32 + lane] = m;
-                cnt += __popc(m);
+            });
+            const uint32_t mw[4] = {m0, m1, m2, m3};
+#pragma unroll
+            for (int wd = 0; wd < 4; wd++) {
+                if (wd < nw) {
+                    smask[wd * 32 + lane] = mw[wd];
+                    cnt += __popc(mw[wd]);
+                }
             }
         } else {
             for (int wd = 0; wd < nw; wd++) smask[wd * 32 + lane] = 0u;
@@ -310,8 +308,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
             double ax = 0.0, ay = 0.0, ed = 0.0;
             double axo, ayo, edot;
             if (MODE == MODE_EXACT64) {
-                for (int e = k - 1; e >= 0; e--) {  // sim/sph.go:343, farthest first
-                    const uint32_t code = (uint32_t)nb[e];
+                for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {  // sim/sph.go:343, farthest first
                     const double d = dist[e].x;
                     const double drk = dist[e].y;  // dF(NNDists[i]/maxR), evaluated by the density pass
                     double rabx, raby, dot;
@@ -325,15 +322,14 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                     ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
                     ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
                     ed = __dadd_rn(ed, __dmul_rn(dot, drk));
-                }
+                });
                 const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
                 axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
                 ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
                 edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
             } else {
                 // the fast form keeps (dF, dF / NNDists) per neighbour
-                for (int e = k - 1; e >= 0; e--) {
-                    const uint32_t code = (uint32_t)nb[e];
+                for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {
                     const double2 dd = dist[e];
                     const uint32_t j = code >> kCodeShift;
                     const double2 vpj = B.vp[j], Q = B.pos[j];
@@ -347,7 +343,7 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                     ax += rabx * w;
                     ay += raby * w;
                     ed += dot * dd.x;
-                }
+                });
                 const double inv_h = 1.0 / hi;
                 const double f = S.mass * S.dfpref * (inv_h * inv_h * inv_h);
                 axo = ax * f + S.accel[0];

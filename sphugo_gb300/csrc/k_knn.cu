@@ -927,13 +927,13 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             // NNDists and q = NNDists/h; q grows with e (the list is sorted), so
             // the entries with q < 0.5 are a prefix of length s
             int s_lo = 0;
-            for (int e = k - 1; e >= 0; e--) {
-                const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, (uint32_t)nb[e]));
+            for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {
+                const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, code));
                 // == __ddiv_rn(d, h); in [0, 1] because d <= h
                 const double x = div_rn_recip(d, h, yh);
                 s_lo += __double_as_longlong(x) < __double_as_longlong(0.5);  // x < 0.5 (x >= 0)
                 dist[e] = make_double2(d, x);
-            }
+            });
             // kernel sums farthest first (sim/sph.go:311-316), each branch of the
             // Monahan kernel in its own loop (no divergent branch per term); the
             // force's dF(q) replaces q in the list
@@ -974,13 +974,13 @@ __global__ void __launch_bounds__(256) k_density(KnnArgs a) {
             // q and 1/NNDists first; then the kernel sums and dF in branch-split
             // loops (q grows with e), leaving (dF, dF / NNDists) for the force
             int s_lo = 0;
-            for (int e = k - 1; e >= 0; e--) {
-                const double d2 = e == k - 1 ? dk2 : nbr_d2(S, B, P, (uint32_t)nb[e]);
+            for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {
+                const double d2 = e == k - 1 ? dk2 : nbr_d2(S, B, P, code);
                 const double y = rsqrt(d2);
                 const double x = fmin(d2 * y * inv_h, 1.0);
                 s_lo += x < 0.5;
                 dist[e] = make_double2(x, y);
-            }
+            });
             double acc = 0.0;
             if (S.kernel == SPH_KERNEL_WENDLAND) {
                 for (int e = k - 1; e >= 0; e--) {

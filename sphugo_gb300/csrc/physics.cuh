@@ -102,6 +102,25 @@ __device__ __forceinline__ float kdf_f32(int kernel, float q) {
     return -(a * a);
 }
 
+// Calls f(e, code) for the neighbour list entries e = k-1 down to 0 (the
+// reference's farthest-first order), reading four codes per load when k is a
+// multiple of four (lists are 16-byte aligned then).
+template <typename F>
+__device__ __forceinline__ void for_each_nbr_desc(const int32_t *nb, int k, F f) {
+    if ((k & 3) == 0) {
+        const int4 *nb4 = reinterpret_cast<const int4 *>(nb);
+        for (int b = (k >> 2) - 1; b >= 0; b--) {
+            const int4 c = nb4[b];
+            f(4 * b + 3, (uint32_t)c.w);
+            f(4 * b + 2, (uint32_t)c.z);
+            f(4 * b + 1, (uint32_t)c.y);
+            f(4 * b, (uint32_t)c.x);
+        }
+    } else {
+        for (int e = k - 1; e >= 0; e--) f(e, (uint32_t)nb[e]);
+    }
+}
+
 // Kahan-compensated FP32 accumulator
 struct KahanF {
     float s = 0.f, c = 0.f;
