@@ -512,12 +512,58 @@ constexpr int kTileCap = 512;  // 9-bit tile slots
 constexpr int kTileRows = 64;
 constexpr int kTileBox = 1024;
 
+// Batcher's odd-even merge sort (K. E. Batcher, "Sorting networks and their
+// applications", 1968) of NS keys in registers, ascending: the network for the
+// next power of two with every comparator that touches a position >= NS left
+// out (those positions would hold +infinity and never move).
+template <int NS>
+struct OddEvenSort {
+    uint32_t (&v)[NS];
+    __device__ __forceinline__ void ce(int i, int j) {
+        if (j < NS) {
+            const uint32_t lo = min(v[i], v[j]);
+            v[j] = max(v[i], v[j]);
+            v[i] = lo;
+        }
+    }
+    template <int LO, int N, int R>
+    __device__ __forceinline__ void merge() {
+        constexpr int M = 2 * R;
+        if constexpr (M < N) {
+            merge<LO, N, M>();
+            merge<LO + R, N, M>();
+#pragma unroll
+            for (int i = LO + R; i + R < LO + N; i += M) ce(i, i + R);
+        } else {
+            ce(LO, LO + R);
+        }
+    }
+    template <int LO, int N>
+    __device__ __forceinline__ void sort() {
+        if constexpr (N > 1 && LO < NS) {
+            sort<LO, N / 2>();
+            sort<LO + N / 2, N / 2>();
+            merge<LO, N, 1>();
+        }
+    }
+    __device__ __forceinline__ void run() {
+        constexpr int P2 = NS <= 32 ? 32 : NS <= 64 ? 64 : 128;
+        sort<0, P2>();
+    }
+};
+
 template <int NR>
 struct TileSmem {
-    static constexpr int LCAP = 24 * NR;  // per-query list capacity (>= 1.5 k)
-    // k <= 80: the k+1 smallest keys are kept in A registers per lane
+    // per-query list capacity: k + 3 or more (k <= 37 for NR = 2); lists
+    // longer than that go to the per-query kernel. 40 for NR = 2 measured
+    // fastest at k = 32 (36 and 38 defer too many queries, 48 sorts more)
+    static constexpr int LCAP = NR == 2 ? 40 : 24 * NR;
+    // k <= 80: the k+1 smallest keys are kept in A registers per lane, for
+    // LCAP <= 40 by sorting the whole list with a network (a fixed 264 or 610
+    // min/max), beyond that by an insertion chain (2 A min/max per entry)
     static constexpr bool REG = NR <= 4;
-    static constexpr int A = NR == 1 ? 18 : NR == 2 ? 38 : 81;
+    static constexpr bool NET = NR <= 2;
+    static constexpr int A = NET ? LCAP : 81;
     float2 rec[kTileCap];             // candidate positions relative to the group origin
     uint32_t code[kTileCap];          // (slot << kCodeShift) | image
     int4 rect[32];                    // per query: cell rectangle at the tile level
@@ -779,31 +825,42 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
             // per list entry (registers only: no divergence, no smem latency chain)
             constexpr int A = TS::A;
             uint32_t arr[A];
-#pragma unroll
-            for (int i = 0; i < A; i++) arr[i] = 0xffffffffu;
             const int m = ok ? cnt : 0;
-            for (int e = 0; e < m; e++) {
-                uint32_t v = sm.list[e][lane];
+            if constexpr (TS::NET) {
 #pragma unroll
-                for (int i = 0; i < A; i++) {
-                    const uint32_t lo = min(arr[i], v);
-                    v = max(arr[i], v);
-                    arr[i] = lo;
+                for (int i = 0; i < A; i++) arr[i] = i < m ? sm.list[i][lane] : 0xffffffffu;
+                if (ok) OddEvenSort<A>{arr}.run();
+            } else {
+#pragma unroll
+                for (int i = 0; i < A; i++) arr[i] = 0xffffffffu;
+                for (int e = 0; e < m; e++) {
+                    uint32_t v = sm.list[e][lane];
+#pragma unroll
+                    for (int i = 0; i < A; i++) {
+                        const uint32_t lo = min(arr[i], v);
+                        v = max(arr[i], v);
+                        arr[i] = lo;
+                    }
                 }
             }
-            float tau = 0.f, nxt = 3.0e38f, prv = 0.f;
+            // arr is ascending: the k-th key is the largest of the first k, the
+            // (k+1)-th the smallest of the rest (reductions rather than
+            // selects at i == k - 1, which the compiler turns into an indexed
+            // load from local memory)
+            uint32_t kth = 0, kprv = 0, knx = 0xffffffffu;
             bool order_ok = true;
 #pragma unroll
             for (int i = 0; i < A; i++) {
-                const float ki = (float)(arr[i] >> 9) * unit;
-                if (i == k - 1) tau = ki;
-                if (i == k) nxt = cnt > k ? ki : 3.0e38f;
-                if (i == k - 2) prv = ki;
+                kth = max(kth, i < k ? arr[i] : 0u);
+                kprv = max(kprv, i < k - 1 ? arr[i] : 0u);
+                knx = min(knx, i >= k ? arr[i] : 0xffffffffu);
                 if (MODE != MODE_MIXED && i > 0 && i < k) {
-                    const float kp = (float)(arr[i - 1] >> 9) * unit;
+                    const float ki = (float)(arr[i] >> 9) * unit, kp = (float)(arr[i - 1] >> 9) * unit;
                     order_ok = order_ok && (ki - kp > 2.f * (kEpsRel * ki + ea));
                 }
             }
+            const float tau = (float)(kth >> 9) * unit, prv = (float)(kprv >> 9) * unit;
+            const float nxt = cnt > k ? (float)(knx >> 9) * unit : 3.0e38f;
             const float et = kEpsRel * tau + ea;
             ok = ok && tau + 3.f * et <= R2 * (1.f - 4.8e-7f);
             ok = ok && (cnt == k || nxt - tau > 2.f * (kEpsRel * nxt + ea));
@@ -813,10 +870,6 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
                 // the mixed form needs the set, with the farthest last (it fixes h):
                 // the entries up to the k-th key in tile (cell) order, which keeps
                 // the force pass's gathers close in memory
-                uint32_t kth = 0;
-#pragma unroll
-                for (int i = 0; i < A; i++)
-                    if (i == k - 1) kth = arr[i];
                 int32_t *out = a.D.nbr + q * k;
                 float *o2 = a.D.d2f + q * k;
                 int o = 0;
