@@ -511,6 +511,7 @@ constexpr int kTileWarps = 4;
 constexpr int kTileCap = 512;  // 9-bit tile slots
 constexpr int kTileRows = 64;
 constexpr int kTileBox = 1024;
+constexpr int kTileCells = 511;  // cells whose record offsets a tile keeps (lane-rectangle scans)
 
 // Batcher's odd-even merge sort (K. E. Batcher, "Sorting networks and their
 // applications", 1968) of NS keys in registers, ascending: the network for the
@@ -569,6 +570,7 @@ struct TileSmem {
     int4 rect[32];                    // per query: cell rectangle at the tile level
     int32_t rx0[kTileRows], rx1[kTileRows], rpre[kTileRows + 1];
     int32_t self[32];                 // tile slot of each query's own record
+    uint16_t cstart[kTileCells + 1];  // first record of each cell (one image block, <= kTileCells cells)
     alignas(16) uint32_t list[LCAP + 1][32];  // per-query keys, one column per query (+ a spare row)
 };
 static_assert(offsetof(TileSmem<1>, list) % 16 == 0 && offsetof(TileSmem<2>, list) % 16 == 0 &&
@@ -593,8 +595,12 @@ __device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t
     if (mine) a.D.defer[base + __popc(bal & lanemask_lt())] = (int32_t)q;
 }
 
+// Register budgets: the FP64 forms with lists of <= 40 entries get 128
+// registers (four blocks per SM, which shared memory allows); the mixed form
+// and longer lists compile without a block minimum (0), which measured
+// spill-free where an explicit minimum of 1 or 4 did not.
 template <int MODE, int NR>
-__global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
+__global__ void __launch_bounds__(kTileWarps * 32, (MODE == MODE_MIXED || NR > 2) ? 0 : 4) k_knn_tile(KnnArgs a) {
     using TS = TileSmem<NR>;
     constexpr int LCAP = TS::LCAP;
     constexpr uint32_t FULL = 0xffffffffu;
@@ -660,8 +666,10 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
         const float ohx = __shfl_sync(FULL, pr.x, 0), olx = __shfl_sync(FULL, pr.z, 0);
         const float ohy = __shfl_sync(FULL, pr.y, 0), oly = __shfl_sync(FULL, pr.w, 0);
         int total = 0;
+        bool rowscan = false;
         if (!defer_all) {
             const int shift = level - sh, Gl = 1 << shift;
+            int ncell_one = INT_MAX;
             sm.rect[lane] = valid ? make_int4(x0 >> sh, x1 >> sh, y0 >> sh, y1 >> sh) : make_int4(1, 0, 1, 0);
             sm.self[lane] = -1;
             __syncwarp();
@@ -734,39 +742,52 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
                             over = true;
                             break;
                         }
-                        const int cbase = j0 - (inc - cnt);  // record t of this chunk is particle cbase + t
-                        for (int t0 = 0; t0 < tot; t0 += 32) {
-                            const int t = t0 + lane;
-                            int src = 0;
+                        if (c <= kTileCells) sm.cstart[c] = (uint16_t)(total + inc - cnt);
+                        // each lane copies its own cell's records (one contiguous
+                        // range), four loads in flight
+                        const int off = total + inc - cnt;  // tile slot of the cell's first record
+                        if (img == 4) {
+                            for (int r0 = 0; r0 < cnt; r0 += 4) {
+                                // relative to the group origin from the float pairs (FP32 only)
+                                float4 rv[4];
 #pragma unroll
-                            for (int b = 16; b > 0; b >>= 1) {
-                                const int iv = __shfl_sync(FULL, inc, src + b - 1);
-                                if (iv <= t) src += b;
-                            }
-                            const int j = __shfl_sync(FULL, cbase, src) + t;
-                            if (t < tot) {
-                                if (img == 4) {
-                                    // relative to the group origin from the float pairs (FP32 only)
-                                    const float4 r = __ldg(&B.rec[j]);
-                                    sm.rec[total + t] = make_float2((r.x - ohx) + (r.z - olx), (r.y - ohy) + (r.w - oly));
-                                } else {
-                                    // an image: its virtual position (q shifted by wx periods) in
-                                    // FP64, relative to the group origin, rounded once to FP32
-                                    const double2 Q = B.pos[j];
-                                    const double qx = wx ? __dadd_rn(Q.x, (double)wx * Lx) : Q.x;
-                                    const double qy = wy ? __dadd_rn(Q.y, (double)wy * Ly) : Q.y;
-                                    sm.rec[total + t] = make_float2(__double2float_rn(__dsub_rn(qx, gx)),
-                                                                    __double2float_rn(__dsub_rn(qy, gy)));
+                                for (int u = 0; u < 4; u++)
+                                    if (r0 + u < cnt) rv[u] = __ldg(&B.rec[j0 + r0 + u]);
+#pragma unroll
+                                for (int u = 0; u < 4; u++) {
+                                    if (r0 + u < cnt) {
+                                        const int j = j0 + r0 + u, t = off + r0 + u;
+                                        sm.rec[t] = make_float2((rv[u].x - ohx) + (rv[u].z - olx),
+                                                                (rv[u].y - ohy) + (rv[u].w - oly));
+                                        sm.code[t] = ((uint32_t)j << kCodeShift) | img;
+                                        if (j >= g0 && j < g0 + 32) sm.self[j - g0] = t;
+                                    }
                                 }
-                                sm.code[total + t] = ((uint32_t)j << kCodeShift) | img;
-                                if (img == 4 && j >= g0 && j < g0 + 32) sm.self[j - g0] = total + t;
+                            }
+                        } else {
+                            // an image: its virtual position (q shifted by wx periods) in
+                            // FP64, relative to the group origin, rounded once to FP32
+                            const double sx = (double)wx * Lx, sy = (double)wy * Ly;
+                            for (int r = 0; r < cnt; r++) {
+                                const double2 Q = B.pos[j0 + r];
+                                const double qx = wx ? __dadd_rn(Q.x, sx) : Q.x;
+                                const double qy = wy ? __dadd_rn(Q.y, sy) : Q.y;
+                                sm.rec[off + r] = make_float2(__double2float_rn(__dsub_rn(qx, gx)),
+                                                              __double2float_rn(__dsub_rn(qy, gy)));
+                                sm.code[off + r] = ((uint32_t)(j0 + r) << kCodeShift) | img;
                             }
                         }
                         total += tot;
                     }
+                    if (lane == 0 && ncell <= kTileCells) sm.cstart[ncell] = (uint16_t)total;
+                    ncell_one = ncell;
                     __syncwarp();
                 }
             }
+            // one image block with few enough cells: each lane scans only the
+            // cells of its own rectangle, row by row (contiguous record ranges)
+            rowscan = (BX0 >> shift) == (BX1 >> shift) && (BY0 >> shift) == (BY1 >> shift) &&
+                      ncell_one <= kTileCells;
             __syncwarp();
             defer_all = over || __any_sync(FULL, valid && sm.self[lane] < 0);
         }
@@ -782,35 +803,42 @@ __global__ void __launch_bounds__(kTileWarps * 32) k_knn_tile(KnnArgs a) {
         const float R2 = valid ? R * R : -1.f;
         const float qs = valid ? 8388608.f / R2 : 0.f;  // key units: R^2 / 2^23
         int cnt = 0;
-        int t = 0;
-        const float4 *rec2 = reinterpret_cast<const float4 *>(sm.rec);  // two records per load
-        for (; t + 4 <= total; t += 4) {
-            float2 c[4];
-            const float4 ab = rec2[t >> 1], cd = rec2[(t >> 1) + 1];
-            c[0] = make_float2(ab.x, ab.y);
-            c[1] = make_float2(ab.z, ab.w);
-            c[2] = make_float2(cd.x, cd.y);
-            c[3] = make_float2(cd.z, cd.w);
-            // branch-free: every record is written to the next free row (a
-            // spare row once the list is full) and counted only when it passes
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const float dx = c[u].x - rqx, dy = c[u].y - rqy;
-                const float d2 = __fmaf_rn(dx, dx, dy * dy);
-                const bool pass = d2 <= R2 && t + u != myself;
-                const uint32_t kq = key23(d2, qs);
-                sm.list[min(cnt, LCAP)][lane] = (kq << 9) | (uint32_t)(t + u);
-                cnt += pass ? 1 : 0;
-            }
-        }
-        for (; t < total; t++) {
-            const float2 c = sm.rec[t];
+        // branch-free: every record is written to the next free row (a spare
+        // row once the list is full) and counted only when it passes
+        auto visit = [&](int t, float2 c) {
             const float dx = c.x - rqx, dy = c.y - rqy;
             const float d2 = __fmaf_rn(dx, dx, dy * dy);
             const bool pass = d2 <= R2 && t != myself;
             const uint32_t kq = key23(d2, qs);
             sm.list[min(cnt, LCAP)][lane] = (kq << 9) | (uint32_t)t;
             cnt += pass ? 1 : 0;
+        };
+        if (rowscan) {
+            // the cells of this query's rectangle: one record range per row
+            // (invalid lanes hold an empty rectangle)
+            const int lx0 = x0 >> sh, lx1 = x1 >> sh;
+            for (int vy = y0 >> sh; vy <= (y1 >> sh); vy++) {
+                const int rr = vy - BY0;
+                const int base = sm.rpre[rr] - sm.rx0[rr];
+                int t = sm.cstart[base + lx0];
+                const int e = sm.cstart[base + lx1 + 1];
+                for (; t + 2 <= e; t += 2) {
+                    visit(t, sm.rec[t]);
+                    visit(t + 1, sm.rec[t + 1]);
+                }
+                if (t < e) visit(t, sm.rec[t]);
+            }
+        } else {
+            int t = 0;
+            const float4 *rec2 = reinterpret_cast<const float4 *>(sm.rec);  // two records per load
+            for (; t + 4 <= total; t += 4) {
+                const float4 ab = rec2[t >> 1], cd = rec2[(t >> 1) + 1];
+                visit(t, make_float2(ab.x, ab.y));
+                visit(t + 1, make_float2(ab.z, ab.w));
+                visit(t + 2, make_float2(cd.x, cd.y));
+                visit(t + 3, make_float2(cd.z, cd.w));
+            }
+            for (; t < total; t++) visit(t, sm.rec[t]);
         }
         bool ok = valid && cnt >= k && cnt <= LCAP;
         // decisions in FP32 with the error bound eps
