@@ -11,8 +11,8 @@ from sphugo_gb300 import sim as S
 pytestmark = pytest.mark.gpu
 
 
-def _sim(n=20_000, precision="Exact"):
-    conf = ics.periodic_config(n, 32, 1e-4, precision)
+def _sim(n=20_000, precision="Exact", k=32):
+    conf = ics.periodic_config(n, k, 1e-4, precision)
     return S.Simulation(conf, *ics.uniform_blast(n, 3))
 
 
@@ -114,11 +114,14 @@ def test_division_sequences_are_correctly_rounded(gpu):
     assert bad.value == 0
 
 
-@pytest.mark.parametrize("precision", ["Exact", "Mixed"])
-def test_group_tiles_match_per_query_search(gpu, precision):
+@pytest.mark.parametrize("precision,k", [("Exact", 32), ("Mixed", 32), ("Exact", 16), ("Mixed", 16),
+                                         ("Exact", 64), ("Mixed", 64)])
+def test_group_tiles_match_per_query_search(gpu, precision, k):
     """The group-tile search (default) and the per-query search return the
-    same exact neighbour sets; in the FP64 form every result is identical."""
-    a, b = _sim(30_000, precision), _sim(30_000, precision)
+    same exact neighbour sets; in the FP64 form every result is identical.
+    k = 16, 32 and 64 take the three list shapes of the tile kernel (24- and
+    40-entry sorting networks, the 81-key insertion chain)."""
+    a, b = _sim(30_000, precision, k), _sim(30_000, precision, k)
     b.SetSearch(False)
     if precision == "Exact":
         a.Step(5)
@@ -139,7 +142,7 @@ def test_group_tiles_match_per_query_search(gpu, precision):
     qa, dfa = a.search_stats()
     qb, dfb = b.search_stats()
     assert qa == qb == 30_000 and dfb == qb
-    assert dfa < 0.2 * qa  # most queries settled by the tiles
+    assert dfa < 0.3 * qa  # most queries settled by the tiles
 
 
 def test_group_tiles_cover_ensemble_boundaries_and_images(gpu):
