@@ -559,11 +559,11 @@ struct TileSmem {
     // longer than that go to the per-query kernel. 40 for NR = 2 measured
     // fastest at k = 32 (36 and 38 defer too many queries, 48 sorts more)
     static constexpr int LCAP = NR == 2 ? 40 : 24 * NR;
-    // k <= 80: the k+1 smallest keys are kept in A registers per lane, for
-    // LCAP <= 40 by sorting the whole list with a network (a fixed 264 or 610
-    // min/max), beyond that by an insertion chain (2 A min/max per entry)
+    // k <= 80: each lane sorts its whole list in registers with a network
+    // (264, 610 or 2112 min/max for LCAP = 24, 40, 96); longer lists take a
+    // shared-memory insertion sort
     static constexpr bool REG = NR <= 4;
-    static constexpr bool NET = NR <= 2;
+    static constexpr bool NET = NR <= 4;
     static constexpr int A = NET ? LCAP : 81;
     float2 rec[kTileCap];             // candidate positions relative to the group origin
     uint32_t code[kTileCap];          // (slot << kCodeShift) | image
