@@ -42,7 +42,7 @@ __device__ __forceinline__ void integrate_one(const SimDev &S, double2 &pos, dou
 
 // The mixed form (the FP64 forms run k_force_fp64 below).
 template <int MODE>
-__global__ void __launch_bounds__(256) k_force(ForceArgs a) {
+__global__ void __launch_bounds__(256, 4) k_force(ForceArgs a) {
     static_assert(MODE == MODE_MIXED, "the FP64 forms run k_force_fp64");
     const int k = a.c.k;
     const PArrays &B = a.B;
@@ -69,13 +69,19 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
             auto pair = [&](uint32_t code) {
                 const uint32_t j = code >> kCodeShift;
                 const uint32_t img = code & 15u;
-                const int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
                 const float4 r = __ldg(&B.rec[j]);
                 // r_AB = (q - offset) - p from float pairs (see the kNN kernel)
-                const float rabx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
-                                   (r.z - (pr.z + (ia > 0 ? dXl : ia < 0 ? -dXl : 0.f)));
-                const float raby = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
-                                   (r.w - (pr.w + (ib > 0 ? dYl : ib < 0 ? -dYl : 0.f)));
+                float rabx, raby;
+                if (img == 4u) {  // no periodic shift (all but the boundary pairs)
+                    rabx = (r.x - pr.x) + (r.z - pr.z);
+                    raby = (r.y - pr.y) + (r.w - pr.w);
+                } else {
+                    const int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
+                    rabx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
+                           (r.z - (pr.z + (ia > 0 ? dXl : ia < 0 ? -dXl : 0.f)));
+                    raby = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
+                           (r.w - (pr.w + (ib > 0 ? dYl : ib < 0 ? -dYl : 0.f)));
+                }
                 const float d2 = __fmaf_rn(rabx, rabx, raby * raby);
                 const float invd = rsqrtf(d2);
                 const float qq = fminf(d2 * invd * inv_hf, 1.f);
@@ -90,8 +96,10 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
                     const float cab = 0.5f * (ci + dj.x);
                     const float rhoab = 0.5f * (rhoi + dj.y);
                     const float hab = 0.5f * (hif + dj.z);
-                    const float mu = dot * hab / (d2 + etasq);
-                    piab = mu * (beta * mu - alpha * cab) / rhoab;
+                    // two-instruction quotients (<= 2 ulp; both denominators are
+                    // normal: d2 + eta^2 >= eta^2, rho_AB > 0)
+                    const float mu = __fdividef(dot * hab, d2 + etasq);
+                    piab = __fdividef(mu * (beta * mu - alpha * cab), rhoab);
                 }
                 const float w = (piab + caf + dj.w) * drk * invd;
                 ax.add(rabx * w);
