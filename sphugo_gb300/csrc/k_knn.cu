@@ -287,18 +287,33 @@ __device__ int select_write(const KnnArgs &a, const SimDev &S, int64_t q, int m,
     return 0;
 }
 
+// Cells holding more than kHeavyCell particles are not scanned whole: they are
+// split into their four children (the next finer level; contiguous ranges of
+// the Morton-ordered table), which are pruned against the radius again. This
+// bounds the work of a sparse query next to a dense region, whose cells at the
+// level chosen from its radius can hold thousands of particles of which only
+// a sliver lies within the radius. Up to kRefineQueue cells wait per warp;
+// when the queue is full a heavy cell is scanned whole.
+constexpr int kHeavyCell = 128;
+constexpr int kRefineQueue = 64;
+__host__ __device__ constexpr size_t knn_warp_bytes(int nr) {
+    return (size_t)32 * nr * 20 + (size_t)kRefineQueue * sizeof(int4);
+}
+
 template <int MODE, int NR>
-__global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
+__global__ void __launch_bounds__(256, 3) k_knn(KnnArgs a) {
     using LS = ListShape<NR>;
     constexpr int CAP = LS::CAP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    // per-warp scratch: exact keys, full FP32 keys, codes, sorted order
-    unsigned char *base = smem_raw + (size_t)w * CAP * 20;
+    // per-warp scratch: exact keys, full FP32 keys, codes, sorted order, and
+    // the queue of heavy cells to refine
+    unsigned char *base = smem_raw + (size_t)w * knn_warp_bytes(NR);
     unsigned long long *sexact = (unsigned long long *)base;
     uint32_t *skey = (uint32_t *)(base + CAP * 8);
     uint32_t *scode = skey + CAP;
     uint32_t *sord = scode + CAP;
+    int4 *rq = (int4 *)(base + CAP * 20);
     const int k = a.c.k;
     const PArrays &B = a.B;
     unsigned fl = 0;
@@ -372,23 +387,30 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
             const int ncell = nx * ny;
             const float inv_nx = 1.f / (float)max(nx, 1);
             m = 0;
-            for (int cb = 0; cb < ncell; cb += 32) {
-                // one cell per lane: its range, image and float-pair constants
-                const int ci = cb + lane;
+            int qn = 0;  // heavy cells waiting in rq (warp-uniform)
+            // One cell per lane (`have`): cell (vx, vy) of the level 2^csh times
+            // the finest, in virtual coordinates (images outside [0, Gl)). The
+            // lane prunes it against the radius, queues it when heavy, else the
+            // warp scans the cells' particles together.
+            auto visit = [&](bool have, int vx, int vy, int csh) {
+                const int cshift = level - csh;  // Gc = 2^cshift cells per axis at this level
+                const int Gc = 1 << cshift;
+                const float cpw = __int_as_float((127 + csh) << 23);  // 2^csh
+                const float CSx = sx0 * cpw, CSy = sy0 * cpw;
                 int cbase = 0, cnt = 0;
                 uint32_t img = 4;
                 float Ax = pr.x, Bx = 0.f, Cx = pr.z, Ay = pr.y, By = 0.f, Cy = pr.w;
-                if (ci < ncell) {
-                    const int oy = (int)(((float)ci + 0.5f) * inv_nx);  // exact: ci, nx < 2^20
-                    const int vx = vx0 + (ci - oy * nx), vy = vy0 + oy;
-                    const int wx = vx >> shift, wy = vy >> shift;       // floor division by 2^shift
-                    const float xlo = (float)vx * Sx, ylo = (float)vy * Sy;
-                    const float dxc = fmaxf(fmaxf(xlo - pxr, pxr - (xlo + Sx)) - tol, 0.f);
-                    const float dyc = fmaxf(fmaxf(ylo - pyr, pyr - (ylo + Sy)) - tol, 0.f);
+                bool heavy = false;
+                if (have) {
+                    const int wx = vx >> cshift, wy = vy >> cshift;  // floor division by 2^cshift
+                    const float xlo = (float)vx * CSx, ylo = (float)vy * CSy;
+                    const float dxc = fmaxf(fmaxf(xlo - pxr, pxr - (xlo + CSx)) - tol, 0.f);
+                    const float dyc = fmaxf(fmaxf(ylo - pyr, pyr - (ylo + CSy)) - tol, 0.f);
                     if (dxc * dxc + dyc * dyc <= R2) {
-                        const uint32_t mo = morton2((uint32_t)(vx & (Gl - 1)), (uint32_t)(vy & (Gl - 1)));
-                        const int j0 = __ldg(a.start + coff + ((int64_t)mo << (2 * sh)));
-                        cnt = __ldg(a.start + coff + ((int64_t)(mo + 1) << (2 * sh))) - j0;
+                        const uint32_t mo = morton2((uint32_t)(vx & (Gc - 1)), (uint32_t)(vy & (Gc - 1)));
+                        const int j0 = __ldg(a.start + coff + ((int64_t)mo << (2 * csh)));
+                        cnt = __ldg(a.start + coff + ((int64_t)(mo + 1) << (2 * csh))) - j0;
+                        heavy = cnt > kHeavyCell && csh > 0;
                         img = (uint32_t)((1 - wx) * 3 + (1 - wy));
                         // image i = -w: hi part of q - i*d exact (Sterbenz) when i = +1,
                         // of p + i*d when i = -1
@@ -397,6 +419,13 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
                         cbase = j0;
                     }
                 }
+                // heavy cells go to the queue while it has room (else they are scanned)
+                const uint32_t hb = __ballot_sync(0xffffffffu, heavy);
+                if (heavy && qn + __popc(hb & lanemask_lt()) < kRefineQueue) {
+                    rq[qn + __popc(hb & lanemask_lt())] = make_int4(vx, vy, csh, 0);
+                    cnt = 0;
+                }
+                qn = min(qn + __popc(hb), kRefineQueue);
                 int inc = cnt;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -438,6 +467,22 @@ __global__ void __launch_bounds__(256) k_knn(KnnArgs a) {
                     }
                     m += __popc(bal);
                 }
+            };
+            for (int cb = 0; cb < ncell; cb += 32) {
+                const int ci = cb + lane;
+                const int oy = (int)(((float)ci + 0.5f) * inv_nx);  // exact: ci, nx < 2^20
+                visit(ci < ncell, vx0 + (ci - oy * nx), vy0 + oy, sh);
+            }
+            // refine the queued heavy cells: up to eight per round, a lane per child
+            while (qn > 0) {
+                const int take = min(qn, 8);
+                __syncwarp();
+                int4 e = make_int4(0, 0, 1, 0);
+                const bool have = lane < 4 * take;
+                if (have) e = rq[qn - take + (lane >> 2)];
+                __syncwarp();  // the entries are read before visit() queues new ones
+                qn -= take;
+                visit(have, 2 * e.x + (lane & 1), 2 * e.y + ((lane >> 1) & 1), e.z - 1);
             }
             if (m < k) {
                 if (R >= Rmax) { fl |= FLAG_KNN_FEW; break; }
@@ -1135,7 +1180,7 @@ static int list_regs(int k) {
     const int need = (3 * k) / 2 + 8;
     return need <= 32 ? 1 : need <= 64 ? 2 : need <= 128 ? 4 : 8;
 }
-static size_t knn_smem(int nr) { return (size_t)(kKnnBlock / 32) * 32 * nr * 20; }
+static size_t knn_smem(int nr) { return (size_t)(kKnnBlock / 32) * knn_warp_bytes(nr); }
 
 template <int MODE, int NR>
 static void knn_attr() {

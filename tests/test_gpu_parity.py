@@ -153,6 +153,28 @@ def test_nonuniform_neighbour_sets_exact(gpu, oracle, kind, n, k):
     assert_bitwise(g, o)
 
 
+@pytest.mark.parametrize("precision", ["Exact", "Mixed"])
+def test_heavy_cells_refined_exact(gpu, oracle, precision):
+    """A binning level far coarser than the automatic one (cells of the dense
+    square hold hundreds of particles) makes the per-query search split heavy
+    cells into their children; the neighbour sets stay exact."""
+    n = 60_000
+    arrs = ics.stress(n, 5)
+    conf = ics.periodic_config(n, 32, 1e-5, precision, grid_level=5)
+    g, o = pair(oracle, conf, arrs)
+    g.SetSearch(False)
+    if precision == "Exact":
+        g.Step(1)
+        o.step(1)
+        assert_bitwise(g, o)
+    else:  # on the same positions (a mixed step moves them off the FP64 ones)
+        g.CalculateForces()
+        o.forces()
+        gi, gdist, gimg = g.neighbours()
+        oi, odist, oimg = o.neighbours()
+        assert np.array_equal(gi, oi) and np.array_equal(gimg, oimg) and np.array_equal(gdist, odist)
+
+
 def normalised_errors(g_state, g_der, o_state, anorm, unorm):
     """Relative density error; |a| and du/dt errors over the per-particle sum
     of neighbour-term magnitudes (a zero normaliser demands a zero error)."""
