@@ -12,6 +12,7 @@ Tolerances:
 import numpy as np
 import pytest
 
+from sphugo_gb300 import _lib as L
 from sphugo_gb300 import ics
 from sphugo_gb300 import sim as S
 
@@ -150,6 +151,38 @@ def test_nonuniform_neighbour_sets_exact(gpu, oracle, kind, n, k):
     g, o = pair(oracle, conf, arrs)
     g.Step(1)
     o.step(1)
+    assert_bitwise(g, o)
+
+
+@pytest.mark.parametrize("k,tiles", [(1, True), (1, False), (2, True), (2, False), (100, True), (128, True),
+                                     (128, False)])
+def test_extreme_neighbour_counts_bitwise(gpu, oracle, k, tiles):
+    """k = 1, 2 (the smallest list shape) and k = 100, 128 (lists beyond the
+    register paths: the tile kernel's shared-memory insertion sort, the
+    per-query kernel's eight-register lists), both search paths, against the
+    oracle. With k = 1 the only density term is F(1) = 0, so rho = 0 and the
+    forces are not finite (the library reports it, the reference computes
+    infinities); with k = 2 one term makes the run blow up within a step. For
+    both only the first evaluation's neighbour sets are compared; k = 100 and
+    128 step three times bit for bit."""
+    n = 6000
+    conf, arrs = blast(n, k=k, seed=7)
+    g, o = pair(oracle, conf, arrs)
+    g.SetSearch(tiles)
+    if k <= 2:
+        if k == 1:
+            with pytest.raises(L.SphError) as e:
+                g.CalculateForces()
+            assert e.value.code == L.SPH_ERR_RANGE
+        else:
+            g.CalculateForces()
+        o.forces()
+        gi, gd, gm = g.neighbours()
+        oi, od, om = o.neighbours()
+        assert np.array_equal(gi, oi) and np.array_equal(gm, om) and np.array_equal(gd, od)
+        return
+    g.Step(3)
+    o.step(3)
     assert_bitwise(g, o)
 
 
