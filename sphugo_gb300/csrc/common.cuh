@@ -60,6 +60,7 @@ struct SimDev {
     float tol;             // absolute slack of the FP32 cell tests
     // FP32 copies used per query (no FP64 instruction in the search's hot path)
     float fs[2];           // finest cell side
+    float fdtc[2];         // dth / finest cell side (the binning's drift in cell units)
     float fimg_h[2], fimg_l[2]; // image shifts as float pairs (hi, lo)
     float flmax;           // max(L)
     float fmag;            // bound on |p + offset| of any particle image (the reference rounds it)
@@ -140,19 +141,11 @@ __device__ __forceinline__ int floordiv(int a, int b) {
     return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
 }
 
-// finest cell coordinate of v on one axis, clamped into the grid
-__device__ __forceinline__ int cell_coord(const SimDev &S, int ax, double v) {
-    double t = __dmul_rn(__dsub_rn(v, S.lo[ax]), S.inv_s[ax]);
-    int G = 1 << S.level;
-    if (!(t >= 0.0)) return 0;
-    if (t >= (double)G) return G - 1;
-    return (int)t;
-}
-
 // FP32 fields of a SimDev from its FP64 grid fields
 __host__ __device__ inline void simdev_floats(SimDev &S) {
     for (int a = 0; a < 2; a++) {
         S.fs[a] = (float)S.s[a];
+        S.fdtc[a] = (float)(S.dth * S.inv_s[a]);
         S.fimg_h[a] = (float)S.dimg[a];
         S.fimg_l[a] = (float)(S.dimg[a] - (double)S.fimg_h[a]);
     }

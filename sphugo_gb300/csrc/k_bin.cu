@@ -80,15 +80,30 @@ __global__ void k_bin(Ctx c, PArrays A, Tables T, int pred) {
          i += (int64_t)gridDim.x * blockDim.x) {
         int s = sim_of(c, i);
         const SimDev &S = c.sims[s];
-        double2 p, vp;
-        double up;
-        predict(S, pred, A.pos[i], A.vel[i], A.acc[i], A.u[i], A.udot[i], A.vp[i], A.up[i], p, vp, up);
-        if (!isfinite(p.x) || !isfinite(p.y)) atomicOr(c.flags, (unsigned)FLAG_NONFINITE);
-        int cx = cell_coord(S, 0, p.x), cy = cell_coord(S, 1, p.y);
+        // The cell of the drifted position, in cell units: the offset from the
+        // grid origin in FP64, rounded once to FP32 (error <= 2^-24 G cells,
+        // 6e-8 L), plus the drift vel * dth in FP32. The exact FP64 drift is
+        // k_permute's; a particle within that error of a cell face may land in
+        // the neighbouring cell, which the searches' slack S.tol (4e-7 L)
+        // covers. The FP64 pipe is the binning's bound: this is 4 FP64
+        // operations per axis instead of about 15.
+        const double2 pos = A.pos[i];
+        float tx = __double2float_rn(__dmul_rn(__dsub_rn(pos.x, S.lo[0]), S.inv_s[0]));
+        float ty = __double2float_rn(__dmul_rn(__dsub_rn(pos.y, S.lo[1]), S.inv_s[1]));
+        if (pred == PRED_DRIFT) {
+            const double2 vel = A.vel[i];
+            tx = __fmaf_rn(__double2float_rn(vel.x), S.fdtc[0], tx);
+            ty = __fmaf_rn(__double2float_rn(vel.y), S.fdtc[1], ty);
+        }
+        if (!isfinite(tx) || !isfinite(ty)) atomicOr(c.flags, (unsigned)FLAG_NONFINITE);
+        const int G = 1 << S.level;
+        const float Gf = (float)G;
+        const int cx = !(tx >= 0.f) ? 0 : tx >= Gf ? G - 1 : (int)tx;
+        const int cy = !(ty >= 0.f) ? 0 : ty >= Gf ? G - 1 : (int)ty;
         // distance outside the periodic domain (the wrap moves at most one axis per step)
         float o = 0.f;
-        if (S.periodic[0]) o = fmaxf(o, (float)fmax(S.lo[0] - p.x, p.x - (S.lo[0] + S.L[0])));
-        if (S.periodic[1]) o = fmaxf(o, (float)fmax(S.lo[1] - p.y, p.y - (S.lo[1] + S.L[1])));
+        if (S.periodic[0]) o = fmaxf(o, fmaxf(-tx, tx - Gf) * S.fs[0]);
+        if (S.periodic[1]) o = fmaxf(o, fmaxf(-ty, ty - Gf) * S.fs[1]);
         if (o > 0.f) atomicMax((int *)&c.sims_rw[s].overshoot, __float_as_int(o * 1.0001f));
         int32_t key = (int32_t)(S.cell_off + morton2(cx, cy));
         T.key[i] = key;
