@@ -277,6 +277,43 @@ def workload_case(kind, n, k, dt, seed, form, steps, grid_level=0):
     return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st, "tune": tune}
 
 
+def mixed_errors(arrays, n, k, dt):
+    """Max and RMS relative errors of the mixed form against the FP64 form
+    (which equals the oracle bit for bit) on identical inputs: the FP64 form
+    runs five steps (so that particles move: viscosity and du/dt terms), then
+    both forms take that state and evaluate the forces once; every particle.
+    rho error relative to rho; |a| and du/dt errors over the particle's sum of
+    the magnitudes of its neighbour terms (a zero sum demands a zero error)."""
+    import numpy as np
+    from sphugo_gb300 import ics
+    from sphugo_gb300 import sim as S
+    sims = {}
+    for form in ("Exact", "Mixed"):
+        s = S.Simulation(ics.periodic_config(n, k, dt, form), *arrays)
+        s.Autotune()  # the cached choice of the timed run
+        sims[form] = s
+    sims["Exact"].Step(5)
+    st = sims["Exact"].state()
+    for s in sims.values():
+        s.set_state(*(st[c] for c in ("x", "y", "vx", "vy", "u", "ax", "ay", "udot")))
+        s.CalculateForces()
+    e, m = sims["Exact"], sims["Mixed"]
+    es, ed, (an, un) = e.state(), e.derived(), e.error_norms()
+    ms, md = m.state(), m.derived()
+    for s in sims.values():
+        s.close()
+
+    def ratio(err, norm):
+        out = np.where(norm > 0, err / np.where(norm > 0, norm, 1.0), np.where(err == 0, 0.0, np.inf))
+        return {"max": float(out.max()), "rms": float(np.sqrt(np.mean(out * out)))}
+    return {
+        "rho": ratio(np.abs(md["rho"] - ed["rho"]), np.abs(ed["rho"])),
+        "accel_normalised": ratio(np.hypot(ms["ax"] - es["ax"], ms["ay"] - es["ay"]), an),
+        "udot_normalised": ratio(np.abs(ms["udot"] - es["udot"]), un),
+        "sample": f"all {n} particles, one force evaluation of both forms on the FP64 form's state after 5 steps",
+    }
+
+
 def e2e_run(sim, steps):
     """set_state from pinned host arrays + step + get_state, every step."""
     import numpy as np
@@ -435,6 +472,7 @@ def run_ours(args, dist):
 
     extras = {}
     if not args.no_extras and dist.rank == 0:
+        from sphugo_gb300 import ics
         for form in ("Fast", "Mixed"):
             s2 = make_sim(n, form, SEED)
             s2.Step(W)
@@ -444,15 +482,18 @@ def run_ours(args, dist):
                 "tune": s2.tune_report, "search_deferred": s2.search_stats()[1]}
             s2.close()
         extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
+        extras["mixed"]["errors_vs_fp64"] = mixed_errors(ics.uniform_blast(n, SEED), n, K_NEIGH, DT)
         ens = {}
         for form in ("Exact", "Mixed"):
             ens[form.lower()] = ensemble_case(form, 5, 256)
         extras["ensemble_256"] = ens
         clu = {f.lower(): workload_case("clustered", 4_194_304, 32, 1e-5, 3, f, 5) for f in ("Exact", "Mixed")}
         clu["mixed_vs_fp64"] = clu["mixed"]["value"] / clu["exact"]["value"]
+        clu["mixed"]["errors_vs_fp64"] = mixed_errors(ics.clustered(4_194_304, 3), 4_194_304, 32, 1e-5)
         extras["clustered_N4194304_k32"] = clu
         stress = {f.lower(): workload_case("stress", 16_777_216, 64, 1e-6, 4, f, 3) for f in ("Exact", "Mixed")}
         stress["mixed_vs_fp64"] = stress["mixed"]["value"] / stress["exact"]["value"]
+        stress["mixed"]["errors_vs_fp64"] = mixed_errors(ics.stress(16_777_216, 4), 16_777_216, 64, 1e-6)
         extras["stress_N16777216_k64"] = stress
 
     cpu = None

@@ -102,6 +102,12 @@ int sph_get_state(sph_handle *h, double *x, double *y, double *vx, double *vy, d
 /* Particle.Rho, C and NNDists[0] (the smoothing length) of the last force
  * evaluation; any pointer may be NULL. */
 int sph_get_derived(sph_handle *h, double *rho, double *c, double *hsml);
+/* Per particle (caller order), the sums of the magnitudes of its neighbour
+ * terms of the last force evaluation: |r_AB| |(Pi + cA + cB) dF / r| |f| for the
+ * acceleration and |v_AB . r_AB dF| |cA m| for du/dt (sim/sph.go:343-398), the
+ * normalisers of the mixed form's error statements. SPH_PREC_FP64 handles
+ * only; any pointer may be NULL. No reference counterpart. */
+int sph_error_norms(sph_handle *h, double *anorm, double *unorm);
 /* Particle.NearestNeighbours / NNDists in the reference layout
  * (sim/core.go:36-38): n*k entries, slot 0 = the farthest neighbour; ids are
  * particle indices in the caller's order; dist may be NULL; img (may be

@@ -797,6 +797,21 @@ int sph_get_derived(sph_handle *h, double *rho, double *c, double *hsml) {
     return SPH_OK;
 }
 
+int sph_error_norms(sph_handle *h, double *anorm, double *unorm) {
+    if (!h) return fail(SPH_ERR_ARG, "null handle");
+    Guard g(h);
+    if (h->mode != MODE_EXACT64) return fail(SPH_ERR_STATE, "sph_error_norms needs an SPH_PREC_FP64 handle");
+    if (!h->uploaded || !h->evaluated || h->n_eval != h->n) return fail(SPH_ERR_STATE, "no force evaluation yet");
+    const int64_t n = h->n;
+    double *d = h->d_io;
+    launch_error_norms(h->ctx(), h->launch(), h->B, h->D, d, d + n);
+    CUDA_TRY(cudaGetLastError());
+    int rc;
+    if ((rc = copy_out(h, anorm, d)) || (rc = copy_out(h, unorm, d + n))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
 int sph_get_neighbours(sph_handle *h, int64_t *ids, double *dist, int32_t *img) {
     if (!h) return fail(SPH_ERR_ARG, "null handle");
     Guard g(h);

@@ -238,6 +238,8 @@ void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Deriv
 void force_init_attrs(int k);
 void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays &A,
                   const Derived &D, int mode, bool integrate);
+void launch_error_norms(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, double *anorm,
+                        double *unorm);
 
 void launch_gather_state(const Ctx &c, const Launch &L, const PArrays &A, double *x, double *y,
                          double *vx, double *vy, double *u, double *ax, double *ay, double *udot);

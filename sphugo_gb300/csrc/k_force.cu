@@ -64,24 +64,11 @@ __global__ void __launch_bounds__(256, 4) k_force(ForceArgs a) {
             const float4 pr = B.rec[q];
             const float4 vi = B.vrec[q];
             const float alpha = S.falpha, beta = S.fbeta, etasq = S.fetasq;
-            const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
             KahanF ax, ay, ed;
             auto pair = [&](uint32_t code) {
                 const uint32_t j = code >> kCodeShift;
-                const uint32_t img = code & 15u;
-                const float4 r = __ldg(&B.rec[j]);
-                // r_AB = (q - offset) - p from float pairs (see the kNN kernel)
-                float rabx, raby;
-                if (img == 4u) {  // no periodic shift (all but the boundary pairs)
-                    rabx = (r.x - pr.x) + (r.z - pr.z);
-                    raby = (r.y - pr.y) + (r.w - pr.w);
-                } else {
-                    const int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
-                    rabx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
-                           (r.z - (pr.z + (ia > 0 ? dXl : ia < 0 ? -dXl : 0.f)));
-                    raby = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
-                           (r.w - (pr.w + (ib > 0 ? dYl : ib < 0 ? -dYl : 0.f)));
-                }
+                float rabx, raby;  // r_AB = (q - offset) - p from float pairs
+                float_pair_rel(S, pr, __ldg(&B.rec[j]), code & 15u, rabx, raby);
                 const float d2 = __fmaf_rn(rabx, rabx, raby * raby);
                 const float invd = rsqrtf(d2);
                 const float qq = fminf(d2 * invd * inv_hf, 1.f);
@@ -414,6 +401,58 @@ void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays
         else k_force_fp64<MODE_FAST64><<<eg, kForceWarps * 32, force_exact_smem(c.k), L.stream>>>(a);
     }
     else k_force<MODE_MIXED><<<grid, block, 0, L.stream>>>(a);
+}
+
+// ------------------------------------------------------------ error norms
+// Per particle, the sums of the magnitudes of its neighbour terms in the
+// acceleration and in du/dt: the normalisers of the mixed form's error
+// statements. Read from the FP64 form's last evaluation (positions, predicted
+// velocities, lists with (NNDists, dF), per-particle (c, rho, h, c^2/(gamma
+// rho))), in the reference's term order (sim/sph.go:343-392, farthest first)
+// and rounding, so that they equal the oracle's norms bit for bit.
+__global__ void k_error_norms(Ctx c, PArrays B, Derived D, double *anorm, double *unorm) {
+    const int k = c.k;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < c.n;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const SimDev &S = c.sims[sim_of(c, q)];
+        const double2 P = B.pos[q], vpi = B.vp[q];
+        const double4 di = D.der[q];  // (c, rho, h, c^2/(gamma rho))
+        const int32_t *nb = D.nbr + q * k;
+        const double2 *dist = D.dist + q * k;
+        double an = 0.0, un = 0.0;
+        for (int e = k - 1; e >= 0; e--) {
+            const uint32_t code = (uint32_t)nb[e];
+            double rabx, raby, dot;
+            pair_geom(S, B, code, P, vpi, rabx, raby, dot);
+            const double d = dist[e].x, drk = dist[e].y;
+            const double4 dj = D.der[code >> kCodeShift];
+            double piab = 0.0;
+            if (dot < 0.0) {
+                const double cab = __dmul_rn(0.5, __dadd_rn(di.x, dj.x));
+                const double rhoab = __dmul_rn(0.5, __dadd_rn(di.y, dj.y));
+                const double hab = __dmul_rn(0.5, __dadd_rn(di.z, dj.z));
+                const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
+                const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, S.etasq));
+                piab = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-S.alpha, cab), mu), __dmul_rn(__dmul_rn(S.beta, mu), mu)),
+                                 rhoab);
+            }
+            const double w = __ddiv_rn(__dmul_rn(__dadd_rn(__dadd_rn(piab, di.w), dj.w), drk), d);
+            an = __dadd_rn(an, __dmul_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby))), fabs(w)));
+            un = __dadd_rn(un, fabs(__dmul_rn(dot, drk)));
+        }
+        const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(di.z, di.z), di.z));
+        const int32_t id = B.id[q];
+        anorm[id] = __dmul_rn(an, fabs(f));
+        unorm[id] = __dmul_rn(un, fabs(__dmul_rn(di.w, S.mass)));
+    }
+}
+
+void launch_error_norms(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, double *anorm,
+                        double *unorm) {
+    const int block = 256;
+    const int64_t need = (c.n + block - 1) / block;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)L.sms * 8));
+    k_error_norms<<<grid, block, 0, L.stream>>>(c, B, D, anorm, unorm);
 }
 
 }  // namespace sphgpu

@@ -121,6 +121,26 @@ __device__ __forceinline__ void for_each_nbr_desc(const int32_t *nb, int k, F f)
     }
 }
 
+// r_AB = (q - offset) - p from the float-pair records of the neighbour (r)
+// and the particle (pr), image code img (4 = no shift): the high parts'
+// difference is exact by Sterbenz for neighbours within a period, so the
+// result carries only the rounding of the low parts (about 2^-48 of the
+// coordinates) and of the final sum.
+__device__ __forceinline__ void float_pair_rel(const SimDev &S, float4 pr, float4 r, uint32_t img, float &rabx,
+                                               float &raby) {
+    if (img == 4u) {
+        rabx = (r.x - pr.x) + (r.z - pr.z);
+        raby = (r.y - pr.y) + (r.w - pr.w);
+    } else {
+        const float dXh = S.fimg_h[0], dXl = S.fimg_l[0], dYh = S.fimg_h[1], dYl = S.fimg_l[1];
+        const int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
+        rabx = ((r.x - (ia > 0 ? dXh : 0.f)) - (ia < 0 ? pr.x - dXh : pr.x)) +
+               (r.z - (pr.z + (ia > 0 ? dXl : ia < 0 ? -dXl : 0.f)));
+        raby = ((r.y - (ib > 0 ? dYh : 0.f)) - (ib < 0 ? pr.y - dYh : pr.y)) +
+               (r.w - (pr.w + (ib > 0 ? dYl : ib < 0 ? -dYl : 0.f)));
+    }
+}
+
 // Kahan-compensated FP32 accumulator
 struct KahanF {
     float s = 0.f, c = 0.f;

@@ -339,6 +339,15 @@ class Simulation:
         L.check(L.load().sph_get_derived(self._h, *[L.dptr(a) for a in arrs]))
         return dict(zip(["rho", "c", "h"], arrs))
 
+    def error_norms(self):
+        """(anorm, unorm): per particle, the sums of the magnitudes of its
+        neighbour terms in the acceleration and du/dt of the last evaluation
+        (FP64 form only); the normalisers of the mixed form's errors."""
+        a = np.empty(self.n)
+        u = np.empty(self.n)
+        L.check(L.load().sph_error_norms(self._h, L.dptr(a), L.dptr(u)))
+        return a, u
+
     def neighbours(self):
         """(ids, NNDists, image codes), each (n, k); slot 0 = farthest."""
         n, k = self.n, self.k

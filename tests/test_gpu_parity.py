@@ -258,6 +258,27 @@ def test_mixed_accuracy_and_exact_sets(gpu, oracle):
     assert u.max() <= 1e-4, u.max()
 
 
+def test_error_norms_match_oracle(gpu, oracle):
+    """The normalisers of the mixed form's error statements (sums of the
+    neighbour-term magnitudes), computed on the device from the FP64 form's
+    evaluation, equal the oracle's bit for bit; other forms refuse."""
+    conf, (x, y, _, _, u) = blast(8000, seed=2)
+    rng = np.random.default_rng(2)
+    vx, vy = rng.normal(0, 0.3, x.size), rng.normal(0, 0.3, x.size)  # approaching pairs: viscosity terms
+    g, o = pair(oracle, conf, (x, y, vx, vy, u))
+    g.CalculateForces()
+    o.forces()
+    ga, gu = g.error_norms()
+    oa, ou = o.norms()
+    assert np.array_equal(ga, oa) and np.array_equal(gu, ou)
+    confm, _ = blast(8000, seed=2, precision="Mixed")
+    m = S.Simulation(confm, x, y, vx, vy, u)
+    m.CalculateForces()
+    with pytest.raises(L.SphError) as e:
+        m.error_norms()
+    assert e.value.code == L.SPH_ERR_STATE
+
+
 def test_mixed_sets_stay_exact_on_own_positions(gpu, oracle):
     """After several mixed steps the positions differ from FP64 ones, but the
     neighbour lists are still the exact lists of the mixed path's positions."""
