@@ -66,6 +66,47 @@ def test_exact_bitwise_after_one_step(gpu, oracle):
     assert_bitwise(g, o)
 
 
+def test_full_size_uniform_blast_steps_0_and_1(gpu, oracle):
+    """The benchmark workload at its full size (N = 1,048,576, k = 32,
+    dt = 2e-5, seed 2): neighbour sets, NNDists, densities and the whole state
+    bit for bit against the oracle after step 0 and after step 1."""
+    n = 1 << 20
+    conf = ics.periodic_config(n, 32, 2e-5, "Exact")
+    g, o = pair(oracle, conf, ics.uniform_blast(n, 2))
+    for step in (1, 2):
+        g.Step(1)
+        o.step(1)
+        assert g.CurrentStep == step
+        assert_bitwise(g, o)
+
+
+def test_full_size_uniform_blast_full_run(gpu, oracle):
+    """The benchmark workload over its whole run (N = 1,048,576, k = 32,
+    dt = 2e-5, seed 2, 200 steps): every state array, the densities and the
+    neighbour sets bit for bit against the oracle at the end (the oracle takes
+    about two minutes on 16 host cores)."""
+    n = 1 << 20
+    conf = ics.periodic_config(n, 32, 2e-5, "Exact")
+    g, o = pair(oracle, conf, ics.uniform_blast(n, 2))
+    g.Step(200)
+    o.step(200)
+    assert g.CurrentStep == 200
+    assert_bitwise(g, o)
+
+
+def test_small_uniform_blast_full_run(gpu, oracle):
+    """The CPU-sized workload over its whole run (N = 10,000, k = 32,
+    dt = 1e-4, seed 1, 100 steps): every state array, the densities and the
+    neighbour sets bit for bit against the oracle at the end."""
+    n = 10_000
+    conf = ics.periodic_config(n, 32, 1e-4, "Exact")
+    g, o = pair(oracle, conf, ics.uniform_blast(n, 1))
+    g.Step(100)
+    o.step(100)
+    assert g.CurrentStep == 100
+    assert_bitwise(g, o)
+
+
 def test_exact_bitwise_after_twenty_steps(gpu, oracle):
     conf, arrs = blast(4000, seed=7)
     g, o = pair(oracle, conf, arrs)
