@@ -320,6 +320,31 @@ def test_error_norms_match_oracle(gpu, oracle):
     assert e.value.code == L.SPH_ERR_STATE
 
 
+def test_mixed_full_size_clustered_within_tolerances(gpu, oracle):
+    """The mixed form's target workload at its full size (clustered, N =
+    4,194,304, k = 32; random velocities so that viscosity and du/dt terms
+    appear): neighbour sets bit-exact and rho, a, du/dt within the stated
+    tolerances against the oracle on the same state."""
+    n = 1 << 22
+    x, y, _, _, u = ics.clustered(n, 3)
+    rng = np.random.default_rng(3)
+    vx, vy = rng.normal(0, 0.3, n), rng.normal(0, 0.3, n)
+    conf = ics.periodic_config(n, 32, 1e-5, "Mixed")
+    g, o = pair(oracle, conf, (x, y, vx, vy, u))
+    g.CalculateForces()
+    o.forces()
+    gi, gd, gm = g.neighbours()
+    oi, od, om = o.neighbours()
+    assert np.array_equal(gi, oi) and np.array_equal(gm, om) and np.array_equal(gd, od)
+    an, un = o.norms()
+    gs, gder, os_ = g.state(), g.derived(), o.state()
+    assert np.array_equal(gder["h"], os_["h"])
+    r, a, ud = normalised_errors(gs, gder, os_, an, un)
+    assert r.max() <= 1e-5, r.max()
+    assert a.max() <= 1e-4, a.max()
+    assert ud.max() <= 1e-4, ud.max()
+
+
 def test_mixed_sets_stay_exact_on_own_positions(gpu, oracle):
     """After several mixed steps the positions differ from FP64 ones, but the
     neighbour lists are still the exact lists of the mixed path's positions."""
