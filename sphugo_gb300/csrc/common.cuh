@@ -115,15 +115,6 @@ struct Ctx {
 // slot range, so a static per-slot index answers with one load.
 __device__ __forceinline__ int sim_of(const Ctx &c, int64_t i) { return c.simidx ? __ldg(c.simidx + i) : 0; }
 
-__device__ __forceinline__ int find_sim(const int64_t *offs, int nsims, int64_t i) {
-    int lo = 0, hi = nsims - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (__ldg(offs + mid) <= i) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
 __device__ __forceinline__ uint32_t part1by1(uint32_t x) {
     x &= 0x0000ffffu;
     x = (x | (x << 8)) & 0x00ff00ffu;
@@ -134,11 +125,6 @@ __device__ __forceinline__ uint32_t part1by1(uint32_t x) {
 }
 __device__ __forceinline__ uint32_t morton2(uint32_t cx, uint32_t cy) {
     return part1by1(cx) | (part1by1(cy) << 1);
-}
-
-__device__ __forceinline__ int floordiv(int a, int b) {
-    int q = a / b;
-    return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
 }
 
 // FP32 fields of a SimDev from its FP64 grid fields

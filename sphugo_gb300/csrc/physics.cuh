@@ -150,7 +150,6 @@ struct KahanF {
         c = (t - s) - y;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
     __device__ __forceinline__ float value_f() const { return s - c; }
 };
 
