@@ -345,6 +345,24 @@ def test_mixed_full_size_clustered_within_tolerances(gpu, oracle):
     assert ud.max() <= 1e-4, ud.max()
 
 
+def test_mixed_long_run_tracks_fp64(gpu):
+    """Over 200 steps the mixed form's trajectory departs from the FP64 one
+    particle by particle (the flow amplifies differences), but its integrals
+    stay with FP64's: total energy, kinetic energy and the density sum."""
+    n = 100_000
+    out = {}
+    for form in ("Exact", "Mixed"):
+        s = S.Simulation(ics.periodic_config(n, 32, 1e-4, form), *ics.uniform_blast(n, 2))
+        s.Step(200)
+        st = s.state()
+        out[form] = (s.TotalEnergy(), float(np.sum(st["vx"] ** 2 + st["vy"] ** 2)), s.TotalDensity())
+        s.close()
+    (e0, k0, r0), (e1, k1, r1) = out["Exact"], out["Mixed"]
+    assert abs(e1 - e0) <= 1e-9 * abs(e0)
+    assert abs(k1 - k0) <= 1e-5 * k0
+    assert abs(r1 - r0) <= 1e-6 * r0
+
+
 def test_mixed_sets_stay_exact_on_own_positions(gpu, oracle):
     """After several mixed steps the positions differ from FP64 ones, but the
     neighbour lists are still the exact lists of the mixed path's positions."""
