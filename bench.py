@@ -273,8 +273,10 @@ def workload_case(kind, n, k, dt, seed, form, steps, grid_level=0):
     sim.Step(2)
     ms = timed(sim, steps)
     st = profile(sim, 2)
+    hbm = sim.memory_bytes()
     sim.close()
-    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st, "tune": tune}
+    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st, "tune": tune,
+            "hbm_bytes": hbm}
 
 
 def mixed_errors(arrays, n, k, dt):
@@ -427,6 +429,7 @@ def run_ours(args, dist):
 
     stages = profile(sim, 3)
     nq, ndef = sim.search_stats()
+    hbm_bytes = sim.memory_bytes()
     lo_frac, visc_frac = pair_statistics(sim, DT / 2)
     work = algorithmic(K_NEIGH, div_cost.value, sqrt_cost.value, lo_frac, visc_frac)
     ncells = 4 ** 10  # auto level for N = 2^20
@@ -479,7 +482,7 @@ def run_ours(args, dist):
             t = timed(s2, K)
             extras[{"Fast": "fp64_fast", "Mixed": "mixed"}[form]] = {
                 "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3),
-                "tune": s2.tune_report, "search_deferred": s2.search_stats()[1]}
+                "tune": s2.tune_report, "search_deferred": s2.search_stats()[1], "hbm_bytes": s2.memory_bytes()}
             s2.close()
         extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
         extras["mixed"]["errors_vs_fp64"] = mixed_errors(ics.uniform_blast(n, SEED), n, K_NEIGH, DT)
@@ -516,7 +519,7 @@ def run_ours(args, dist):
             "roofline": roofline, "cpu_baseline": cpu, "tolerances": TOLERANCES,
             "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value,
                             "fp64_div_slots": div_cost.value, "fp64_sqrt_slots": sqrt_cost.value}, "forms": extras,
-            "tune": tune_report,
+            "tune": tune_report, "hbm_bytes": hbm_bytes,
             "search": {"queries": nq, "deferred_to_per_query": ndef,
                        "path": "group tiles + per-query for deferred" if ndef < nq else "per-query"},
         }

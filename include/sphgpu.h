@@ -108,6 +108,10 @@ int sph_get_derived(sph_handle *h, double *rho, double *c, double *hsml);
  * normalisers of the mixed form's error statements. SPH_PREC_FP64 handles
  * only; any pointer may be NULL. No reference counterpart. */
 int sph_error_norms(sph_handle *h, double *anorm, double *unorm);
+/* Device memory the handle holds, in bytes: state and evaluation arrays,
+ * neighbour lists, cell tables and scratch (not the on-demand export buffer of
+ * sph_get_neighbours). No reference counterpart. */
+int sph_memory_bytes(sph_handle *h, int64_t *bytes);
 /* Particle.NearestNeighbours / NNDists in the reference layout
  * (sim/core.go:36-38): n*k entries, slot 0 = the farthest neighbour; ids are
  * particle indices in the caller's order; dist may be NULL; img (may be

@@ -91,6 +91,7 @@ struct sph_handle {
     size_t io_doubles = 0;
     void *d_nbr_io = nullptr; // neighbour export staging (lazy)
     std::vector<void *> allocs;
+    std::vector<size_t> alloc_bytes;  // sizes of allocs, entry by entry
     std::mutex mu;
 
     Ctx ctx() const {
@@ -127,6 +128,7 @@ int dalloc(sph_handle *h, T **p, size_t count) {
                     std::string("cudaMalloc: ") + cudaGetErrorString(e));
     }
     h->allocs.push_back(q);
+    h->alloc_bytes.push_back(std::max<size_t>(count, 1) * sizeof(T));
     *p = (T *)q;
     return SPH_OK;
 }
@@ -136,6 +138,7 @@ void dfree(sph_handle *h, void *p) {
     for (size_t i = 0; i < h->allocs.size(); i++)
         if (h->allocs[i] == p) {
             h->allocs.erase(h->allocs.begin() + (long)i);
+            h->alloc_bytes.erase(h->alloc_bytes.begin() + (long)i);
             break;
         }
     cudaFree(p);
@@ -794,6 +797,15 @@ int sph_get_derived(sph_handle *h, double *rho, double *c, double *hsml) {
     if ((rc = copy_out(h, rho, d)) || (rc = copy_out(h, c, d + n)) || (rc = copy_out(h, hsml, d + 2 * n)))
         return rc;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return SPH_OK;
+}
+
+int sph_memory_bytes(sph_handle *h, int64_t *bytes) {
+    if (!h || !bytes) return fail(SPH_ERR_ARG, "bad argument");
+    Guard g(h);
+    size_t t = 0;
+    for (size_t b : h->alloc_bytes) t += b;
+    *bytes = (int64_t)t;
     return SPH_OK;
 }
 

@@ -339,6 +339,12 @@ class Simulation:
         L.check(L.load().sph_get_derived(self._h, *[L.dptr(a) for a in arrs]))
         return dict(zip(["rho", "c", "h"], arrs))
 
+    def memory_bytes(self) -> int:
+        """Device memory this simulation holds (bytes)."""
+        b = C.c_int64()
+        L.check(L.load().sph_memory_bytes(self._h, C.byref(b)))
+        return b.value
+
     def error_norms(self):
         """(anorm, unorm): per particle, the sums of the magnitudes of its
         neighbour terms in the acceleration and du/dt of the last evaluation
@@ -439,6 +445,12 @@ class Ensemble:
 
     def search_stats(self) -> tuple:
         return _search_stats(self._h)
+
+    def memory_bytes(self) -> int:
+        """Device memory the ensemble holds (bytes)."""
+        b = C.c_int64()
+        L.check(L.load().sph_memory_bytes(self._h, C.byref(b)))
+        return b.value
 
     def state(self) -> dict:
         names = ["x", "y", "vx", "vy", "u", "ax", "ay", "udot"]

@@ -176,3 +176,16 @@ def test_truncated_checkpoint_leaves_the_state(gpu, tmp_path):
     assert b.CurrentStep == 1
     for key in before:
         assert np.array_equal(before[key], after[key]), key
+
+
+def test_memory_bytes_counts_the_handle(gpu):
+    """The device memory a handle reports covers at least its state and
+    neighbour lists, stays far below the device, and grows when particles are
+    appended past the allocated capacity."""
+    a = _sim(20_000)
+    mb = a.memory_bytes()
+    assert 20_000 * (32 * 4 + 2 * 100) < mb < 1 << 31
+    x = np.random.default_rng(1).random(40_000)
+    y = np.ascontiguousarray(x[::-1])
+    L.check(gpu.sph_append(a._h, x.size, L.dptr(x), L.dptr(y), None, None, None, None))
+    assert a.memory_bytes() > mb
