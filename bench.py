@@ -132,7 +132,9 @@ def max_over_ranks(values):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms; the summary
+    keeps the samples taken inside the marked timed region (the nearest ones
+    when the region is shorter than the sampling interval)."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -141,24 +143,35 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (arrival time, line)
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
+            return
+        deadline = time.time() + 5.0  # sampling is running before the timed region starts
+        while not self.lines and time.time() < deadline and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
 
     def stop(self):
         if self.proc:
-            time.sleep(0.25)
+            time.sleep(0.1)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -166,7 +179,14 @@ class ClockSampler:
                 self.proc.kill()
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.t0 is not None and self.t1 is not None and lines:
+            inside = [x for x in lines if self.t0 <= x[0] <= self.t1 + 0.05]
+            if not inside:  # shorter than the interval: the samples nearest the region
+                mid = 0.5 * (self.t0 + self.t1)
+                inside = sorted(lines, key=lambda x: abs(x[0] - mid))[:2]
+            lines = inside
+        for _, ln in lines:
             f = [v.strip() for v in ln.split(",")]
             if len(f) < 7:
                 continue
@@ -382,7 +402,7 @@ def run_reference(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="override the particle count (testing only)")
@@ -421,7 +441,9 @@ def run_ours(args, dist):
     clk = ClockSampler(dist.local)
     clk.start()
     dist.barrier()
+    clk.mark_start()
     ms = timed(sim, K)
+    clk.mark_end()
     dist.barrier()
     clocks = clk.stop()
     ms_max = dist.max(ms)
