@@ -1029,8 +1029,10 @@ __device__ __forceinline__ double nbr_d2(const SimDev &S, const PArrays &B, doub
     return dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
 }
 
+// five resident blocks (48 registers): the FP64 forms' first loop waits on the
+// neighbour gathers, and more resident warps hide them (2.06 -> 2.02 ms at N = 1M)
 template <int MODE>
-__global__ void __launch_bounds__(256) k_density(KnnArgs a) {
+__global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
     const int k = a.c.k;
     const PArrays &B = a.B;
     unsigned fl = 0;
