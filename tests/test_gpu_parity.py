@@ -264,8 +264,11 @@ def normalised_errors(g_state, g_der, o_state, anorm, unorm):
     return rho_err, acc, ud
 
 
-def test_fast64_within_1e12(gpu, oracle):
-    conf, (x, y, _, _, u) = blast(3000, seed=5, precision="Fast")
+@pytest.mark.parametrize("n", [3000, 1 << 20])
+def test_fast64_within_1e12(gpu, oracle, n):
+    """The FMA form within 1e-12 of the oracle after a step, also at the
+    benchmark's full size."""
+    conf, (x, y, _, _, u) = blast(n, seed=5, precision="Fast")
     rng = np.random.default_rng(5)
     vx, vy = rng.normal(0, 0.3, x.size), rng.normal(0, 0.3, x.size)  # viscosity on about half the pairs
     g, o = pair(oracle, conf, (x, y, vx, vy, u))
