@@ -410,6 +410,31 @@ def test_ensemble_equals_independent_runs(gpu, oracle):
         assert d[0] == pytest.approx(od[0], rel=1e-13) and d[1] == pytest.approx(od[1], rel=1e-13)
 
 
+def test_ensemble_full_size_equals_oracle(gpu, oracle):
+    """The benchmark's ensemble at its full size (256 simulations of 1,000 to
+    65,536 particles, 3.83M in all, one graph per step): after two steps every
+    simulation's state, densities and neighbour ids equal the oracle's run of
+    that simulation alone, bit for bit."""
+    confs, arrays = ics.make_ensemble(precision="Exact")
+    e = S.Ensemble(confs, arrays)
+    e.Step(2)
+    est, eder = e.state(), e.derived()
+    eids, _, _ = e.neighbours()
+    off = e.offsets
+    for s in range(len(confs)):
+        n = off[s + 1] - off[s]
+        o = oracle.OracleSim(oracle_params(oracle, confs[s], n), *arrays[s])
+        o.step(2)
+        os_ = o.state()
+        sl = slice(off[s], off[s + 1])
+        for k in STATE:
+            assert np.array_equal(est[k][sl], os_[k]), (s, k)
+        assert np.array_equal(eder["rho"][sl], os_["rho"]), s
+        oi, _, _ = o.neighbours()
+        assert np.array_equal(eids[sl] - off[s], oi), s
+        o.close()
+
+
 @pytest.mark.parametrize("precision", ["Exact", "Fast", "Mixed"])
 def test_deterministic_across_runs(gpu, precision):
     """The binning orders each cell's particles by their previous slot, so
