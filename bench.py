@@ -1,18 +1,30 @@
 #!/usr/bin/env python3
 """Particle-steps/s of sphugo's 2D SPH step on GB300.
 
-Workload (the plain-FP64-at-scale case): N = 1,048,576 particles uniform in the
-periodic unit box, blast u = 10 inside r < 0.1 (else 1), k = 32, Monahan
-kernel, gamma 5/3, alpha 1, beta 2, dt = 2e-5, seeded SplitMix64 inputs.
+Headline workload (the configuration the metric is quoted on): N = 4,194,304
+particles drawn from a seeded mixture of 64 Gaussian blobs (centres uniform in
+the periodic unit box, sigma log-uniform in [0.005, 0.05]) plus a 20 %
+uniform background, u = 10 within one sigma of a blob centre (else 1), zero
+velocities, k = 32, Monahan kernel, gamma 5/3, alpha 1, beta 2, dt = 1e-5;
+the workload's full run is 50 steps.
+
 `value` is the plain FP64 drop-in (SPH_PREC_FP64, bit-exact with the
-reference's arithmetic) timed with CUDA events on the library's stream over K
-steps after W warm-up steps, inputs resident in HBM (state > 1 GB, larger than
-L2). `e2e` times the same steps through the public C ABI with the whole state
-copied host->device and back every step from pinned host buffers. Extra
-lines of the JSON report the FP64-fast and mixed forms and the 256-simulation
-ensemble, each against the stated tolerances that the test-suite enforces.
+reference's arithmetic), timed with CUDA events on the library's stream over K
+steps after W warm-up steps, inputs resident in HBM (state and neighbour lists
+of several GB, larger than L2). `e2e` times the same steps through the public
+C ABI with the whole state copied host->device and back every step from pinned
+host buffers. `mixed` is the mixed form (FP32 relative-coordinate Kahan sums,
+FP64 kNN decisions, smoothing lengths and integrator) on the same workload:
+its rate, its ratio to the FP64 form, and the max / RMS relative errors of
+rho, a and du/dt against the FP64 form, stated after five steps and after the
+workload's full 50-step run. `forms` adds the uniform blast at N = 1,048,576,
+the 256-simulation ensemble and the N = 16,777,216, k = 64 stress case.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the reference's algorithm on the host cores: the
+oracle's restatement of the reference's tree search and step (no GPU library
+is loaded), on the same workload, config and metric.
 
 Under torchrun (N > 1) every rank advances its own replica (a single
 simulation does not shard without a halo exchange): value = all ranks'
@@ -23,6 +35,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -33,13 +46,28 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_DEFAULT = 1_048_576
-K_NEIGH = 32
-DT = 2e-5
-SEED = 2
+# the headline workload: clustered blobs, N = 2^22, k = 32, dt = 1e-5, seed 3, 50-step run
+HEAD_KIND, HEAD_N, HEAD_K, HEAD_DT, HEAD_SEED, HEAD_RUN = "clustered", 4_194_304, 32, 1e-5, 3, 50
 METRIC = "particle-steps/s on 1 GB300: mixed/batched vs plain FP64 GPU at stated rel. error"
 TOLERANCES = {"neighbour_sets": "bit-exact", "fp64": "bit-exact", "fp64_fast": 1e-12,
               "mixed_rho": 1e-5, "mixed_accel_normalised": 1e-4, "mixed_udot_normalised": 1e-4}
+FORM_NAMES = {"Exact": "SPH_PREC_FP64 (bit-exact)", "Fast": "SPH_PREC_FP64_FAST (FMA, <=1e-12)",
+              "Mixed": "SPH_PREC_MIXED (FP32 relative-coordinate Kahan sums, FP64 kNN decisions/h/integrator)"}
+HBM_FALLBACK_GBS = 6800.0
+
+
+def head_config(n):
+    """The workload's `config`, identical in both arms."""
+    return {"workload": f"clustered 64 blobs + 20% background N={n} k={HEAD_K} periodic unit box dt={HEAD_DT}",
+            "n": n, "k": HEAD_K, "parallelism": "replicas",
+            "l2": "inputs larger than L2 (state and neighbour lists of several GB)"}
+
+
+def auto_level(n):
+    """The library's automatic binning level (one to four particles per finest cell)."""
+    lv = math.floor(0.5 * math.log2(max(n, 2) / 2.0) + 0.5)
+    return int(min(max(lv, 1), 14))
+
 
 # Algorithmic work per particle and force evaluation. Streaming stages count
 # HBM bytes. FP64 stages count the FP64 operations of the reference's own
@@ -202,43 +230,57 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def ncu_traffic(kernel, form, n):
-    """DRAM bytes per launch of a stage's kernel from the committed ncu
-    summary (profiles/ncu_traffic.json), for the same form and size."""
+def ncu_entry(stage, form, kind):
+    """The committed ncu capture of a stage's kernel (profiles/ncu_traffic.json):
+    key stage/form/workload kind; None when there is none."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            tab = json.load(f)
+            return json.load(f).get(f"{stage}/{form.lower()}/{kind}")
     except (OSError, ValueError):
         return None
-    ent = tab.get(f"{kernel}/{form.lower()}/{n}")
-    return ent.get("dram_bytes_per_launch") if ent else None
 
 
-def ncu_field(stage, form, n, field):
-    """Another figure of the committed ncu summary for a stage (or None)."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            ent = json.load(f).get(f"{stage}/{form.lower()}/{n}")
-    except (OSError, ValueError):
-        return None
-    return ent.get(field) if ent else None
+def ncu_traffic(stage, form, kind, n):
+    """DRAM bytes per launch of a stage at n particles: the capture's own
+    figure scaled by particle count (the stages stream per-particle data and
+    gather neighbours from L2, so traffic grows in proportion), and a note of
+    where the figure comes from."""
+    ent = ncu_entry(stage, form, kind)
+    if not ent or not ent.get("dram_bytes_per_launch"):
+        return None, None
+    scale = n / ent["n"]
+    note = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of {ent['kernel']} on the {kind} workload at "
+            f"N={ent['n']} (commit {ent.get('commit', '?')}, profiles/ncu_traffic.json), x{scale:g} for N={n}")
+    return ent["dram_bytes_per_launch"] * scale, note
 
 
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return json.load(f)
-    except OSError:
+    except (OSError, ValueError):
         return {}
 
 
-def make_sim(n, precision, seed, tune=True):
-    """The workload's simulation, autotuned (the tuner caches its choice)."""
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) and its source."""
+    p = measured_peaks()
+    for key in ("hbm_gbs", "hbm_GBps", "hbm_copy_gbs"):
+        if isinstance(p.get(key), (int, float)) and p[key] > 0:
+            return float(p[key]), "MEASURED_PEAKS.json " + key
+    return HBM_FALLBACK_GBS, "fallback (MEASURED_PEAKS.json absent): 6.8 TB/s, an earlier GB300 copy measurement"
+
+
+def library_inputs(kind, n, seed):
+    from sphugo_gb300 import ics
+    return {"clustered": ics.clustered, "stress": ics.stress, "blast": ics.uniform_blast}[kind](n, seed)
+
+
+def make_sim(kind, n, k, dt, seed, form, tune=True):
+    """A workload's simulation, autotuned (the tuner caches its choice)."""
     from sphugo_gb300 import ics
     from sphugo_gb300 import sim as S
-    conf = ics.periodic_config(n, K_NEIGH, DT, precision)
-    arrs = ics.uniform_blast(n, seed)
-    sim = S.Simulation(conf, *arrs)
+    sim = S.Simulation(ics.periodic_config(n, k, dt, form), *library_inputs(kind, n, seed))
     sim.tune_report = sim.Autotune() if tune else None
     return sim
 
@@ -259,81 +301,117 @@ def profile(sim, steps=3):
 
 
 def ensemble_case(form, steps, nsims):
-    """256 independent simulations: one graph per ensemble step vs one by one."""
+    """256 independent simulations: one graph per ensemble step, against the
+    same simulations as separate handles (each on its own stream). Two
+    baselines: every handle's step enqueued back to back with one wait per
+    ensemble step (sph_step_async, then sph_synchronize on each), and the
+    plain blocking sph_step per handle."""
+    from sphugo_gb300 import _lib as L
     from sphugo_gb300 import ics
     from sphugo_gb300 import sim as S
+    lib = L.load()
     confs, arrays = ics.make_ensemble(nsims=nsims, precision=form)
     ntot = sum(len(a[0]) for a in arrays)
     e = S.Ensemble(confs, arrays)
+    tune = e.Autotune()
     e.Step(2)
     ms = timed(e, steps)
     e.close()
     sims = [S.Simulation(c, *a) for c, a in zip(confs, arrays)]
     for s in sims:
+        s.Autotune()  # cached per size class, as the ensemble's own choice
         s.Step(2)
     t0 = time.perf_counter()
     for _ in range(steps):
         for s in sims:
+            L.check(lib.sph_step_async(s._h, 1))
+        for s in sims:
+            L.check(lib.sph_synchronize(s._h))
+    sep_async = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s in sims:
             s.Step(1)
-    sep = time.perf_counter() - t0
+    sep_sync = time.perf_counter() - t0
     for s in sims:
         s.close()
     graph = ntot * steps / (ms / 1e3)
-    one = ntot * steps / sep
-    return {"n_total": ntot, "sims": nsims, "graph": graph, "one_by_one": one, "ratio": graph / one}
+    one = ntot * steps / sep_async
+    return {"n_total": ntot, "sims": nsims, "graph": graph, "one_by_one": one, "ratio": graph / one,
+            "one_by_one_blocking": ntot * steps / sep_sync, "ratio_vs_blocking": graph * sep_sync / (ntot * steps),
+            "tune": tune,
+            "baseline": "each simulation its own handle and stream, every handle's step enqueued back to back, "
+                        "one wait per ensemble step"}
 
 
-def workload_case(kind, n, k, dt, seed, form, steps, grid_level=0):
-    from sphugo_gb300 import ics
-    from sphugo_gb300 import sim as S
-    arrs = {"clustered": ics.clustered, "stress": ics.stress}[kind](n, seed)
-    conf = ics.periodic_config(n, k, dt, form, grid_level=grid_level)
-    sim = S.Simulation(conf, *arrs)
-    tune = sim.Autotune()
-    sim.Step(2)
-    ms = timed(sim, steps)
-    st = profile(sim, 2)
-    hbm = sim.memory_bytes()
-    sim.close()
-    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st, "tune": tune,
-            "hbm_bytes": hbm}
-
-
-def mixed_errors(arrays, n, k, dt):
+def errors_on_state(st, n, k, dt):
     """Max and RMS relative errors of the mixed form against the FP64 form
-    (which equals the oracle bit for bit) on identical inputs: the FP64 form
-    runs five steps (so that particles move: viscosity and du/dt terms), then
-    both forms take that state and evaluate the forces once; every particle.
-    rho error relative to rho; |a| and du/dt errors over the particle's sum of
-    the magnitudes of its neighbour terms (a zero sum demands a zero error)."""
+    (which equals the oracle bit for bit) when both evaluate the forces of
+    the same state once; every particle. rho error relative to rho; |a| and
+    du/dt errors over the particle's sum of the magnitudes of its neighbour
+    terms (a zero sum demands a zero error)."""
     import numpy as np
     from sphugo_gb300 import ics
     from sphugo_gb300 import sim as S
-    sims = {}
+    out = {}
     for form in ("Exact", "Mixed"):
-        s = S.Simulation(ics.periodic_config(n, k, dt, form), *arrays)
+        s = S.Simulation(ics.periodic_config(n, k, dt, form), st["x"], st["y"], st["vx"], st["vy"], st["u"])
         s.Autotune()  # the cached choice of the timed run
-        sims[form] = s
-    sims["Exact"].Step(5)
-    st = sims["Exact"].state()
-    for s in sims.values():
         s.set_state(*(st[c] for c in ("x", "y", "vx", "vy", "u", "ax", "ay", "udot")))
         s.CalculateForces()
-    e, m = sims["Exact"], sims["Mixed"]
-    es, ed, (an, un) = e.state(), e.derived(), e.error_norms()
-    ms, md = m.state(), m.derived()
-    for s in sims.values():
+        out[form] = (s.state(), s.derived(), s.error_norms() if form == "Exact" else None)
         s.close()
+    (es, ed, (an, un)), (ms, md, _) = out["Exact"], out["Mixed"]
 
     def ratio(err, norm):
-        out = np.where(norm > 0, err / np.where(norm > 0, norm, 1.0), np.where(err == 0, 0.0, np.inf))
-        return {"max": float(out.max()), "rms": float(np.sqrt(np.mean(out * out)))}
+        r = np.where(norm > 0, err / np.where(norm > 0, norm, 1.0), np.where(err == 0, 0.0, np.inf))
+        return {"max": float(r.max()), "rms": float(np.sqrt(np.mean(r * r)))}
     return {
         "rho": ratio(np.abs(md["rho"] - ed["rho"]), np.abs(ed["rho"])),
         "accel_normalised": ratio(np.hypot(ms["ax"] - es["ax"], ms["ay"] - es["ay"]), an),
         "udot_normalised": ratio(np.abs(ms["udot"] - es["udot"]), un),
-        "sample": f"all {n} particles, one force evaluation of both forms on the FP64 form's state after 5 steps",
     }
+
+
+def mixed_errors(kind, n, k, dt, seed, fp64_steps=5, run_steps=None):
+    """The mixed form's stated errors on a workload: on the FP64 form's state
+    after `fp64_steps` steps (particles moving: viscosity and du/dt terms
+    active), and, with `run_steps`, on the mixed form's own state at the end
+    of the workload's full run."""
+    from sphugo_gb300 import ics
+    from sphugo_gb300 import sim as S
+    arrays = library_inputs(kind, n, seed)
+    res = {}
+    s = S.Simulation(ics.periodic_config(n, k, dt, "Exact"), *arrays)
+    s.Autotune()
+    s.Step(fp64_steps)
+    st = s.state()
+    s.close()
+    res["after_fp64_steps"] = errors_on_state(st, n, k, dt)
+    res["after_fp64_steps"]["sample"] = (f"all {n} particles, one force evaluation of both forms on the FP64 "
+                                         f"form's state after {fp64_steps} steps")
+    if run_steps:
+        m = S.Simulation(ics.periodic_config(n, k, dt, "Mixed"), *arrays)
+        m.Autotune()
+        m.Step(run_steps)
+        st = m.state()
+        m.close()
+        res["after_full_run"] = errors_on_state(st, n, k, dt)
+        res["after_full_run"]["sample"] = (f"all {n} particles, one force evaluation of both forms on the mixed "
+                                           f"form's state at the end of its full {run_steps}-step run")
+    return res
+
+
+def workload_case(kind, n, k, dt, seed, form, steps):
+    sim = make_sim(kind, n, k, dt, seed, form)
+    sim.Step(2)
+    ms = timed(sim, steps)
+    st = profile(sim, 2)
+    hbm = sim.memory_bytes()
+    nq, nd = sim.search_stats()
+    sim.close()
+    return {"value": n * steps / (ms / 1e3), "ms_per_step": ms / steps, "stages_ms": st, "tune": sim.tune_report,
+            "hbm_bytes": hbm, "search_deferred": nd}
 
 
 def e2e_run(sim, steps):
@@ -362,17 +440,22 @@ def e2e_run(sim, steps):
     return dt, 8 * 8 * n, 8 * 8 * n
 
 
-def cpu_baseline(n, steps, threads, warm=1):
-    """The oracle's faithful tree path (restating the reference's Step) on host cores."""
+def cpu_tree_run(n, steps, threads, warm):
+    """The oracle's faithful restatement of the reference's Step (tree build,
+    tree kNN with the sorted queue, density, force, leapfrog) on host cores,
+    on the headline workload built by the oracle's own copy of the recipe
+    (no GPU library is loaded). Returns seconds for `steps` regular steps
+    after `warm` warm-up steps (step 0 evaluates the forces twice)."""
     from oracle import oracle as O
-    from sphugo_gb300 import ics
-    x, y, vx, vy, u = ics.uniform_blast(n, SEED)
-    s = O.OracleSim(O.make_params(n, K_NEIGH, knn_mode=O.KNN_TREE, threads=threads, alpha=1.0, beta=2.0,
-                                  dth=DT / 2), x, y, vx, vy, u)
-    s.step(warm)  # step 0 evaluates forces twice; time regular steps only
+    x, y, vx, vy, u = O.clustered(n, HEAD_SEED)
+    s = O.OracleSim(O.make_params(n, HEAD_K, knn_mode=O.KNN_TREE, threads=threads, alpha=1.0, beta=2.0,
+                                  dth=HEAD_DT / 2), x, y, vx, vy, u)
+    s.step(warm)
     t0 = time.perf_counter()
     s.step(steps)
-    return time.perf_counter() - t0
+    secs = time.perf_counter() - t0
+    s.close()
+    return secs
 
 
 def run_reference(args, dist):
@@ -380,19 +463,19 @@ def run_reference(args, dist):
     if dist.rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    n = args.n or N_DEFAULT
+    n = args.n or HEAD_N
     warm = max(1, args.warmup)
     steps = max(1, args.steps)
-    secs = cpu_baseline(n, steps, threads, warm=warm)
+    secs = cpu_tree_run(n, steps, threads, warm)
     v = n * steps / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64)",
-        "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}",
-                   "n": n, "k": K_NEIGH, "form": "reference tree search, FP64"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded SplitMix64 clustered blobs)",
+        "config": head_config(n), "form": "the reference's tree search and step, FP64 (oracle restatement)",
         "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} full steps of N={n} after {warm} warm-up steps"},
+                         "sample": f"{steps} full steps of the N={n} workload after {warm} warm-up steps, "
+                                   f"OpenMP over the per-particle loops"},
         "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -402,7 +485,7 @@ def run_reference(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="override the particle count (testing only)")
@@ -420,21 +503,39 @@ def main():
         dist.close()
 
 
+def stage_rooflines(stages, work, n, form, level, slot_peak, hbm):
+    roof = {}
+    for st, t in stages.items():
+        w = work[st]
+        entry = {"ms": t}
+        if "fp64_slots" in w and form != "Mixed":
+            entry.update(bound="fp64", unit="G FP64-slot/s", achieved=w["fp64_slots"] * n / (t * 1e-3) / 1e9,
+                         peak=slot_peak)
+        else:
+            b = w["bytes"] * n if w["bytes"] else 16 * 4 ** level
+            entry.update(bound="hbm", unit="GB/s", achieved=b / (t * 1e-3) / 1e9, peak=hbm)
+        entry["frac"] = entry["achieved"] / entry["peak"]
+        if st == "knn":
+            # no HBM or FP roofline binds the search: it is issue- and latency-bound
+            entry["binding"] = "instruction issue / shared-memory and L2 latency"
+        roof[st] = entry
+    return roof
+
+
 def run_ours(args, dist):
     from sphugo_gb300 import _lib as L
     from sphugo_gb300 import build
     build.build()
     lib = L.load()
-    n = args.n or N_DEFAULT
+    n = args.n or HEAD_N
     K, W = max(1, args.steps), max(3, args.warmup)
     fp64_pk, fp32_pk, div_cost, sqrt_cost = C.c_double(0), C.c_double(0), C.c_double(0), C.c_double(0)
     L.check(lib.sph_probe_peaks(C.byref(fp64_pk), C.byref(fp32_pk), C.byref(div_cost), C.byref(sqrt_cost)))
+    hbm, hbm_src = hbm_peak()
+    slot_peak = fp64_pk.value / 2 * 1e3  # G FP64 FMA issue slots per second
 
     form = {"exact": "Exact", "fast": "Fast", "mixed": "Mixed"}[args.form]
-    form_name = {"Exact": "SPH_PREC_FP64 (bit-exact)", "Fast": "SPH_PREC_FP64_FAST (FMA, <=1e-12)",
-                 "Mixed": "SPH_PREC_MIXED (FP32 relative-coordinate Kahan sums, FP64 kNN decisions/h/integrator)"}[form]
-    head_form = form
-    sim = make_sim(n, form, SEED + 1000 * dist.rank)
+    sim = make_sim(HEAD_KIND, n, HEAD_K, HEAD_DT, HEAD_SEED + 1000 * dist.rank, form)
     tune_report = sim.tune_report
     sim.Step(W)
     kernels = int(lib.sph_kernels_per_step(sim._h))
@@ -452,96 +553,75 @@ def run_ours(args, dist):
     stages = profile(sim, 3)
     nq, ndef = sim.search_stats()
     hbm_bytes = sim.memory_bytes()
-    lo_frac, visc_frac = pair_statistics(sim, DT / 2)
-    work = algorithmic(K_NEIGH, div_cost.value, sqrt_cost.value, lo_frac, visc_frac)
-    ncells = 4 ** 10  # auto level for N = 2^20
-    peaks = measured_peaks()
-    hbm_peak = peaks.get("hbm_gbs")
-    slot_peak = fp64_pk.value / 2 * 1e3  # G FP64 FMA issue slots per second
-    roof = {}
-    for st, t in stages.items():
-        w = work[st]
-        entry = {"ms": t}
-        if "fp64_slots" in w and form != "Mixed":
-            entry.update(bound="fp64", unit="G FP64-slot/s", achieved=w["fp64_slots"] * n / (t * 1e-3) / 1e9,
-                         peak=slot_peak)
-        else:
-            b = w["bytes"] * n if w["bytes"] else 16 * ncells
-            entry.update(bound="hbm", unit="GB/s", achieved=b / (t * 1e-3) / 1e9, peak=hbm_peak)
-        if entry.get("peak"):
-            entry["frac"] = entry["achieved"] / entry["peak"]
-        if st == "knn":
-            # no HBM or FP roofline binds the search: it is issue- and latency-bound
-            entry["binding"] = "instruction issue / shared-memory latency"
-            issue = ncu_field("knn", form, n, "issue_active_frac")
-            if issue is not None:
-                entry["ncu_issue_active_frac"] = issue
-        roof[st] = entry
+    lo_frac, visc_frac = pair_statistics(sim, HEAD_DT / 2)
+    work = algorithmic(HEAD_K, div_cost.value, sqrt_cost.value, lo_frac, visc_frac)
+    level = auto_level(n) + int((tune_report or {}).get("level_delta", 0))
+    roof = stage_rooflines(stages, work, n, form, level, slot_peak, hbm)
     dom = max(stages, key=stages.get)
     d = roof[dom]
-    traffic = ncu_traffic(dom, form, n)
+    traffic, traffic_note = ncu_traffic(dom, form, HEAD_KIND, n)
     roofline = {"kernel": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
-                "unit": d["unit"], "frac": d.get("frac"), "traffic": traffic,
-                "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                "unit": d["unit"], "frac": d["frac"], "traffic": traffic,
+                "traffic_unit": "bytes per launch", "traffic_source": traffic_note,
                 "peak_source": ("FP64 FMA issue rate from the device probe run by this bench (2 flops per slot; "
-                                "MEASURED_PEAKS.json has no FP64 figure)" if d["bound"] == "fp64"
-                                else "MEASURED_PEAKS.json hbm_gbs"),
+                                "MEASURED_PEAKS.json has no FP64 figure)" if d["bound"] == "fp64" else hbm_src),
                 "fp64_costs": {"div_slots": div_cost.value, "sqrt_slots": sqrt_cost.value,
                                "q_below_half": lo_frac, "approaching_pairs": visc_frac},
                 "stages": roof}
 
-    dt, h2d, d2h = e2e_run(sim, max(3, K // 2))
-    e2e = {"value": n * max(3, K // 2) / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+    e2e_steps = max(3, K // 2)
+    dt, h2d, d2h = e2e_run(sim, e2e_steps)
+    e2e = {"value": n * e2e_steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
     sim.close()
 
+    mixed = None
+    if dist.rank == 0 and form == "Exact":
+        sm = make_sim(HEAD_KIND, n, HEAD_K, HEAD_DT, HEAD_SEED, "Mixed")
+        sm.Step(W)
+        t = timed(sm, K)
+        mstages = profile(sm, 3)
+        mixed = {"value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": mstages,
+                 "roofline_stages": stage_rooflines(mstages, work, n, "Mixed", level, slot_peak, hbm),
+                 "tune": sm.tune_report, "search_deferred": sm.search_stats()[1], "hbm_bytes": sm.memory_bytes()}
+        sm.close()
+        mixed["mixed_vs_fp64"] = mixed["value"] / value * dist.world
+        mixed["errors_vs_fp64"] = mixed_errors(HEAD_KIND, n, HEAD_K, HEAD_DT, HEAD_SEED, 5, HEAD_RUN)
+
     extras = {}
     if not args.no_extras and dist.rank == 0:
-        from sphugo_gb300 import ics
-        for form in ("Fast", "Mixed"):
-            s2 = make_sim(n, form, SEED)
-            s2.Step(W)
-            t = timed(s2, K)
-            extras[{"Fast": "fp64_fast", "Mixed": "mixed"}[form]] = {
-                "value": n * K / (t / 1e3), "ms_per_step": t / K, "stages_ms": profile(s2, 3),
-                "tune": s2.tune_report, "search_deferred": s2.search_stats()[1], "hbm_bytes": s2.memory_bytes()}
-            s2.close()
-        extras["mixed_vs_fp64"] = extras["mixed"]["value"] / value * dist.world
-        extras["mixed"]["errors_vs_fp64"] = mixed_errors(ics.uniform_blast(n, SEED), n, K_NEIGH, DT)
-        ens = {}
-        for form in ("Exact", "Mixed"):
-            ens[form.lower()] = ensemble_case(form, 5, 256)
-        extras["ensemble_256"] = ens
-        clu = {f.lower(): workload_case("clustered", 4_194_304, 32, 1e-5, 3, f, 5) for f in ("Exact", "Mixed")}
-        clu["mixed_vs_fp64"] = clu["mixed"]["value"] / clu["exact"]["value"]
-        clu["mixed"]["errors_vs_fp64"] = mixed_errors(ics.clustered(4_194_304, 3), 4_194_304, 32, 1e-5)
-        extras["clustered_N4194304_k32"] = clu
+        blast = {f.lower(): workload_case("blast", 1_048_576, 32, 2e-5, 2, f, 20) for f in ("Exact", "Fast", "Mixed")}
+        blast["mixed_vs_fp64"] = blast["mixed"]["value"] / blast["exact"]["value"]
+        blast["mixed"]["errors_vs_fp64"] = mixed_errors("blast", 1_048_576, 32, 2e-5, 2)
+        extras["uniform_blast_N1048576_k32"] = blast
+        extras["ensemble_256"] = {f.lower(): ensemble_case(f, 5, 256) for f in ("Exact", "Mixed")}
         stress = {f.lower(): workload_case("stress", 16_777_216, 64, 1e-6, 4, f, 3) for f in ("Exact", "Mixed")}
         stress["mixed_vs_fp64"] = stress["mixed"]["value"] / stress["exact"]["value"]
-        stress["mixed"]["errors_vs_fp64"] = mixed_errors(ics.stress(16_777_216, 4), 16_777_216, 64, 1e-6)
+        stress["mixed"]["errors_vs_fp64"] = mixed_errors("stress", 16_777_216, 64, 1e-6, 4)
         extras["stress_N16777216_k64"] = stress
 
     cpu = None
     if not args.no_cpu and dist.rank == 0:
         threads = os.cpu_count() or 1
-        ncpu = n
-        secs = cpu_baseline(ncpu, 2, threads)
-        cpu = {"value": ncpu * 2 / secs, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-               "sample": f"2 regular steps of the same workload (N={ncpu}) through the oracle's tree path"}
+        secs = cpu_tree_run(n, 2, threads, 1)
+        cpu = {"value": n * 2 / secs, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": f"2 regular steps of the same workload (N={n}) through the oracle's restatement of the "
+                         f"reference's tree search and step, after step 0"}
 
     if dist.rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": dist.world, "steps": K,
             "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if head_form != "Mixed" else "f32+f64", "data": "synthetic (seeded SplitMix64 uniform blast)",
-            "config": {"workload": f"uniform-blast N={n} k={K_NEIGH} periodic unit box dt={DT}, {head_form.lower()} form",
-                       "n": n, "k": K_NEIGH, "form": form_name, "parallelism": "replicas",
-                       "l2": "inputs larger than L2 (state + neighbour lists > 1 GB)"},
+            "vs_baseline": None, "dtype": "f64" if form != "Mixed" else "f32+f64",
+            "data": "synthetic (seeded SplitMix64 clustered blobs)",
+            "config": head_config(n), "form": FORM_NAMES[form],
             "clocks": clocks, "e2e": e2e, "gpu_launches": kernels * K, "kernels_per_step": kernels,
-            "roofline": roofline, "cpu_baseline": cpu, "tolerances": TOLERANCES,
+            "roofline": roofline, "cpu_baseline": cpu, "mixed": mixed,
+            "mixed_vs_fp64": mixed["mixed_vs_fp64"] if mixed else None, "tolerances": TOLERANCES,
             "peaks_probe": {"fp64_tflops": fp64_pk.value, "fp32_tflops": fp32_pk.value,
-                            "fp64_div_slots": div_cost.value, "fp64_sqrt_slots": sqrt_cost.value}, "forms": extras,
-            "tune": tune_report, "hbm_bytes": hbm_bytes,
+                            "fp64_div_slots": div_cost.value, "fp64_sqrt_slots": sqrt_cost.value,
+                            "hbm_gbs": hbm, "hbm_source": hbm_src},
+            "forms": extras, "tune": tune_report, "hbm_bytes": hbm_bytes,
             "search": {"queries": nq, "deferred_to_per_query": ndef,
                        "path": "group tiles + per-query for deferred" if ndef < nq else "per-query"},
         }

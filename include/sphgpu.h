@@ -126,6 +126,14 @@ int sph_step(sph_handle *h, int32_t nsteps);
 /* sim/sph.go:403 CalculateForces on the current positions and predicted
  * velocities / energies (without integrating). */
 int sph_forces(sph_handle *h);
+/* sph_step without the wait: enqueues nsteps steps on the handle's stream
+ * and returns. Device-side errors of those steps (kNN, sentinel, range) are
+ * reported by the next sph_synchronize, sph_step or sph_forces. Lets a caller
+ * that drives many handles keep them all queued (Step itself blocks,
+ * sim/sph.go:64-198). No reference counterpart. */
+int sph_step_async(sph_handle *h, int32_t nsteps);
+/* Waits for the handle's queued work and reports any device-side error it
+ * raised (the status sph_step would have returned). */
 int sph_synchronize(sph_handle *h);
 int32_t sph_current_step(const sph_handle *h);
 int64_t sph_num_particles(const sph_handle *h);
@@ -220,7 +228,8 @@ int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, 
  * else SPH_ERR_ARG. The first call on a device looks up the scratch's device
  * address and sets kernel attributes, so make it before any stream capture.
  * All calls share the scratch: calls that overlap on the GPU (other threads
- * or streams) race, so serialise them. p->precision is ignored. */
+ * or streams) race, so serialise them. p->precision and p->grid_level are
+ * ignored (the binning level follows n, at most 2^7 cells per axis). */
 #define SPH_NOALLOC_MAX_N 8192
 #define SPH_NOALLOC_MAX_K 32
 int sph_density_noalloc(const sph_params *p, const double *x, const double *y, int32_t n, int64_t *nbr_ids,

@@ -18,6 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
 SRC = os.path.join(HERE, "sph_oracle.c")
+SOURCES = [SRC, os.path.join(HERE, "workloads.c")]
 
 KERNEL_MONAHAN = 0
 KERNEL_WENDLAND = 1
@@ -29,11 +30,10 @@ DBL_MAX = sys.float_info.max
 def build(force: bool = False) -> str:
     """Compiles the oracle with contraction off (a*b+c stays two roundings)."""
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-        os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "sph_oracle.h"))
-    ):
+    deps = SOURCES + [os.path.join(HERE, "sph_oracle.h")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, deps)):
         cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
-               "-shared", "-o", LIB_PATH, SRC, "-lm"]
+               "-shared", "-o", LIB_PATH, *SOURCES, "-lm"]
         subprocess.run(cmd, check=True)
     return LIB_PATH
 
@@ -92,6 +92,13 @@ def lib():
         for f in (L.orc_kernel_fpref, L.orc_kernel_dfpref):
             f.argtypes = [C.c_int]
             f.restype = C.c_double
+        L.orc_ic_uniform_blast.argtypes = [C.c_int64, C.c_uint64, C.c_double, C.c_double, C.c_double] + [dp] * 5
+        L.orc_ic_clustered.argtypes = [C.c_int64, C.c_uint64, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_double] + [dp] * 5
+        L.orc_ic_stress.argtypes = [C.c_int64, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_double,
+                                    C.c_double] + [dp] * 5
+        L.orc_ic_ensemble.argtypes = [C.c_int32, C.c_uint64, C.c_int64, C.c_int64, C.c_double, C.c_double,
+                                      i64p, dp]
         _lib = L
     return _lib
 
@@ -255,3 +262,36 @@ def tree_count_outside(x, y):
 
 def hypot(p, q):
     return lib().orc_hypot(p, q)
+
+
+# ---- seeded synthetic workloads (workloads.c), the same arrays as the
+# library's sph_ic_* generators
+
+
+def _ic(fn, n, *args):
+    a = [np.empty(n) for _ in range(5)]
+    rc = fn(n, *args, *a)
+    if rc:
+        raise ValueError(f"initial-condition recipe rejected its arguments (status {rc})")
+    return a
+
+
+def uniform_blast(n, seed, u_bg=1.0, u_blast=10.0, r_blast=0.1):
+    return _ic(lib().orc_ic_uniform_blast, n, seed, u_bg, u_blast, r_blast)
+
+
+def clustered(n, seed, nblobs=64, sig_min=0.005, sig_max=0.05, f_bg=0.2, u_bg=1.0, u_core=10.0):
+    return _ic(lib().orc_ic_clustered, n, seed, nblobs, sig_min, sig_max, f_bg, u_bg, u_core)
+
+
+def stress(n, seed, side=0.1, f_in=0.99, u_bg=1.0, u_hot=100.0, r_hot=0.01):
+    return _ic(lib().orc_ic_stress, n, seed, side, f_in, u_bg, u_hot, r_hot)
+
+
+def ensemble_sizes(nsims, seed, nmin=1000, nmax=65536, ublo=5.0, ubhi=50.0):
+    counts = np.empty(nsims, np.int64)
+    ub = np.empty(nsims)
+    rc = lib().orc_ic_ensemble(nsims, seed, nmin, nmax, ublo, ubhi, counts, ub)
+    if rc:
+        raise ValueError(f"ensemble recipe rejected its arguments (status {rc})")
+    return counts, ub

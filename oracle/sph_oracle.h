@@ -132,6 +132,18 @@ void orc_para_ramp(int index, uint8_t *rgb);  /* gx/graphics.go:156-164 */
 void orc_render(int64_t n, const double *x, const double *y, const double *rho, double mass,
                 const int64_t *order, int W, int H, uint8_t *rgba);
 
+/* Seeded synthetic initial conditions (workloads.c); value for value the
+ * library's sph_ic_* generators, so that the CPU baseline builds its inputs
+ * without the GPU library. */
+int orc_ic_uniform_blast(int64_t n, uint64_t seed, double u_bg, double u_blast, double r_blast, double *x,
+                         double *y, double *vx, double *vy, double *u);
+int orc_ic_clustered(int64_t n, uint64_t seed, int32_t nblobs, double sig_min, double sig_max, double f_bg,
+                     double u_bg, double u_core, double *x, double *y, double *vx, double *vy, double *u);
+int orc_ic_stress(int64_t n, uint64_t seed, double side, double f_in, double u_bg, double u_hot, double r_hot,
+                  double *x, double *y, double *vx, double *vy, double *u);
+int orc_ic_ensemble(int32_t nsims, uint64_t seed, int64_t nmin, int64_t nmax, double ublo, double ubhi,
+                    int64_t *counts, double *u_blast);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,8 @@ PREC_FP64_FAST = 2
 EXPORTS = [
     "sph_default_params", "sph_abi_version", "sph_last_error", "sph_device_count",
     "sph_create", "sph_ens_create", "sph_destroy", "sph_upload", "sph_set_state",
-    "sph_get_state", "sph_get_derived", "sph_error_norms", "sph_memory_bytes", "sph_get_neighbours", "sph_step", "sph_forces",
+    "sph_get_state", "sph_get_derived", "sph_error_norms", "sph_memory_bytes", "sph_get_neighbours", "sph_step",
+    "sph_step_async", "sph_forces",
     "sph_synchronize", "sph_current_step", "sph_num_particles", "sph_host_register",
     "sph_host_unregister", "sph_diagnostics", "sph_ic_uniform_blast", "sph_ic_clustered",
     "sph_ic_stress", "sph_ic_ensemble", "sph_config_default", "sph_config_load",
@@ -117,6 +118,7 @@ def load() -> C.CDLL:
     L.sph_memory_bytes.argtypes = [vp, i64p]
     L.sph_get_neighbours.argtypes = [vp, i64p, dp, i32p]
     L.sph_step.argtypes = [vp, C.c_int32]
+    L.sph_step_async.argtypes = [vp, C.c_int32]
     L.sph_forces.argtypes = [vp]
     L.sph_synchronize.argtypes = [vp]
     L.sph_current_step.argtypes = [vp]

@@ -873,11 +873,28 @@ int sph_forces(sph_handle *h) {
     return check_flags(h);
 }
 
+int sph_step_async(sph_handle *h, int32_t nsteps) {
+    if (!h || nsteps < 0) return fail(SPH_ERR_ARG, "bad handle or step count");
+    Guard g(h);
+    if (!h->uploaded) return fail(SPH_ERR_STATE, "sph_step_async before sph_upload");
+    int rc = ensure_graphs(h);
+    if (rc) return rc;
+    for (int32_t s = 0; s < nsteps; s++) {
+        if (h->step == 0) CUDA_TRY(cudaGraphLaunch(h->g_init, h->stream));
+        CUDA_TRY(cudaGraphLaunch(h->g_step, h->stream));
+        h->step++;
+    }
+    if (nsteps > 0) {
+        h->evaluated = true;
+        h->n_eval = h->n;
+    }
+    return SPH_OK;
+}
+
 int sph_synchronize(sph_handle *h) {
     if (!h) return fail(SPH_ERR_ARG, "null handle");
     Guard g(h);
-    CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return SPH_OK;
+    return check_flags(h);
 }
 
 int sph_host_register(void *ptr, int64_t bytes) {
@@ -1152,15 +1169,18 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
 
 // ---- checkpoint / resume: header, then the state arrays in storage order
 namespace {
+constexpr uint32_t kCkptVersion = 3;
+
 struct CkptHeader {
     char magic[8];      // "SPHGPUCK"
-    uint32_t version;   // 2
+    uint32_t version;   // kCkptVersion
     uint32_t mode;
     int64_t n;
     int32_t nsims, k, step, level_delta;
     uint64_t params_hash;
     float theta, hgrow;  // search shape (the mixed form's sums follow its visiting order)
     int32_t tile, pad;   // search path (group tiles or per query)
+    uint64_t payload_hash;  // FNV-1a of the state arrays as stored
 };
 
 uint64_t fnv1a(const void *p, size_t len, uint64_t hsh = 1469598103934665603ull) {
@@ -1185,6 +1205,36 @@ std::vector<ArrayRef> state_arrays(sph_handle *h) {
     return {{A.pos, 16 * n}, {A.vel, 16 * n}, {A.vp, 16 * n}, {A.acc, 16 * n}, {A.u, 8 * n},
             {A.up, 8 * n},   {A.udot, 8 * n}, {A.id, 4 * n},  {A.hprev, 4 * n}};
 }
+
+// A checkpoint's payload is checked on the host before anything reaches the
+// device: the kernels index the caller's order by `id` (gathers write rho[id],
+// neighbour lists, diagnostics), so ids outside a simulation's own slot range
+// would become out-of-bounds device writes. Checked: the payload hash, that
+// the ids of every simulation are a permutation of its slot range, finite
+// non-negative previous smoothing lengths (the search's radius guess) and a
+// valid search shape.
+int check_checkpoint(const sph_handle *h, const CkptHeader &hd, const std::vector<std::vector<char>> &bufs) {
+    uint64_t ph = 1469598103934665603ull;
+    for (const std::vector<char> &b : bufs) ph = fnv1a(b.data(), b.size(), ph);
+    if (ph != hd.payload_hash) return fail(SPH_ERR_ARG, "checkpoint payload does not match its hash (corrupt file)");
+    const int64_t n = h->n;
+    const int32_t *id = (const int32_t *)bufs[7].data();
+    const float *hprev = (const float *)bufs[8].data();
+    std::vector<unsigned char> seen((size_t)n, 0);
+    for (int s = 0; s < h->nsims; s++)
+        for (int64_t i = h->offs[s]; i < h->offs[s + 1]; i++) {
+            const int64_t v = id[i];
+            if (v < h->offs[s] || v >= h->offs[s + 1] || seen[(size_t)v])
+                return fail(SPH_ERR_ARG, "checkpoint particle ids are not a permutation of each simulation's range");
+            seen[(size_t)v] = 1;
+        }
+    for (int64_t i = 0; i < n; i++)
+        if (!(hprev[i] >= 0.f && hprev[i] < 3.0e38f)) return fail(SPH_ERR_ARG, "checkpoint smoothing lengths invalid");
+    if (!(hd.theta > 0.f && hd.theta < 64.f) || !(hd.hgrow > 0.f && hd.hgrow < 64.f) || (hd.tile != 0 && hd.tile != 1) ||
+        hd.level_delta < -kMaxLevel || hd.level_delta > kMaxLevel || hd.step < 0)
+        return fail(SPH_ERR_ARG, "checkpoint search settings out of range");
+    return SPH_OK;
+}
 }  // namespace
 
 int sph_save(sph_handle *h, const char *path) {
@@ -1194,7 +1244,7 @@ int sph_save(sph_handle *h, const char *path) {
     CkptHeader hd;
     memset(&hd, 0, sizeof hd);
     memcpy(hd.magic, "SPHGPUCK", 8);
-    hd.version = 2;
+    hd.version = kCkptVersion;
     hd.mode = (uint32_t)h->mode;
     hd.n = h->n;
     hd.nsims = h->nsims;
@@ -1205,16 +1255,20 @@ int sph_save(sph_handle *h, const char *path) {
     hd.theta = h->tune.theta;
     hd.hgrow = h->tune.hgrow;
     hd.tile = h->tune.tile;
+    const std::vector<ArrayRef> arrays = state_arrays(h);
+    std::vector<std::vector<char>> bufs(arrays.size());
+    uint64_t ph = 1469598103934665603ull;
+    for (size_t i = 0; i < arrays.size(); i++) {
+        bufs[i].resize(arrays[i].bytes);
+        CUDA_TRY(cudaMemcpyAsync(bufs[i].data(), arrays[i].dev, arrays[i].bytes, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        ph = fnv1a(bufs[i].data(), bufs[i].size(), ph);
+    }
+    hd.payload_hash = ph;
     std::ofstream f(path, std::ios::binary | std::ios::trunc);
     if (!f) return fail(SPH_ERR_ARG, std::string("cannot write ") + path);
     f.write((const char *)&hd, sizeof hd);
-    std::vector<char> buf;
-    for (const ArrayRef &a : state_arrays(h)) {
-        buf.resize(a.bytes);
-        CUDA_TRY(cudaMemcpyAsync(buf.data(), a.dev, a.bytes, cudaMemcpyDeviceToHost, h->stream));
-        CUDA_TRY(cudaStreamSynchronize(h->stream));
-        f.write(buf.data(), (std::streamsize)a.bytes);
-    }
+    for (const std::vector<char> &b : bufs) f.write(b.data(), (std::streamsize)b.size());
     if (!f) return fail(SPH_ERR_ARG, std::string("write failed: ") + path);
     return SPH_OK;
 }
@@ -1226,12 +1280,13 @@ int sph_load(sph_handle *h, const char *path) {
     if (!f) return fail(SPH_ERR_ARG, std::string("cannot read ") + path);
     CkptHeader hd;
     f.read((char *)&hd, sizeof hd);
-    if (!f || memcmp(hd.magic, "SPHGPUCK", 8) != 0 || hd.version != 2)
-        return fail(SPH_ERR_ARG, "not a version-2 SPH checkpoint");
+    if (!f || memcmp(hd.magic, "SPHGPUCK", 8) != 0 || hd.version != kCkptVersion)
+        return fail(SPH_ERR_ARG, "not a version-3 SPH checkpoint");
     if (hd.n != h->n || hd.nsims != h->nsims || hd.k != h->k || hd.mode != (uint32_t)h->mode ||
         hd.params_hash != params_hash(h))
         return fail(SPH_ERR_ARG, "checkpoint was written by a handle with other parameters or sizes");
     // read the whole payload first: a truncated file leaves the handle untouched
+    int rc;
     const std::vector<ArrayRef> arrays = state_arrays(h);
     std::vector<std::vector<char>> bufs(arrays.size());
     for (size_t i = 0; i < arrays.size(); i++) {
@@ -1239,7 +1294,7 @@ int sph_load(sph_handle *h, const char *path) {
         f.read(bufs[i].data(), (std::streamsize)arrays[i].bytes);
         if (!f) return fail(SPH_ERR_ARG, "truncated checkpoint");
     }
-    int rc;
+    if ((rc = check_checkpoint(h, hd, bufs))) return rc;
     if (hd.level_delta != h->level_delta && (rc = apply_levels(h, hd.level_delta))) return rc;
     if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow || hd.tile != h->tune.tile) {
         h->tune.theta = hd.theta;

@@ -43,7 +43,8 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 struct DeviceSetup {
     bool done = false;
     unsigned char *ptr = nullptr;  // device address of g_noalloc_scratch
-    int sms = 0, blocks_per_sm = 1;
+    int sms = 0;
+    int blocks_per_sm[kNoAllocMaxK + 1] = {};  // search launch shape by k (0: not measured yet)
 };
 std::mutex g_setup_mu;
 DeviceSetup g_setup[64];
@@ -107,9 +108,12 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
         return nfail(SPH_ERR_ARG, "sph_density_noalloc: unknown kernel");
     const double *axes[2] = {p->hor, p->vert};
     for (int a = 0; a < 2; a++) {
-        if (axes[a][0] == -DBL_MAX ? axes[a][1] != DBL_MAX : !(axes[a][1] > axes[a][0]))
+        if (axes[a][0] == -DBL_MAX ? axes[a][1] != DBL_MAX
+                                   : !(axes[a][1] > axes[a][0]) || !std::isfinite(axes[a][1] - axes[a][0]))
             return nfail(SPH_ERR_ARG, "sph_density_noalloc: bad periodic bounds");
     }
+    if (!std::isfinite(p->dth) || !std::isfinite(p->gamma) || !std::isfinite(p->mass))
+        return nfail(SPH_ERR_ARG, "sph_density_noalloc: non-finite parameter");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
         cudaGetLastError();
@@ -130,9 +134,11 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
             knn_init_attrs();
             g_setup[dev].ptr = (unsigned char *)ptr;
             cudaDeviceGetAttribute(&g_setup[dev].sms, cudaDevAttrMultiProcessorCount, dev);
-            g_setup[dev].blocks_per_sm = std::max(1, knn_occupancy_blocks(128, p->k + 16, MODE_EXACT64));
             g_setup[dev].done = true;
         }
+        // the search's resident blocks per SM depend on k (its list shape)
+        if (!g_setup[dev].blocks_per_sm[p->k])
+            g_setup[dev].blocks_per_sm[p->k] = std::max(1, knn_occupancy_blocks(128, p->k + 16, MODE_EXACT64));
         ds = g_setup[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -161,7 +167,8 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     int64_t *d_offs = cv.take<int64_t>(2);
     unsigned *d_flags = cv.take<unsigned>(1);
 
-    // constants of this call (grid level capped to the scratch's cell table)
+    // constants of this call: the automatic binning level for n, capped to
+    // the scratch's cell table (p->grid_level is not used)
     SimDev S;
     memset(&S, 0, sizeof S);
     double l = std::floor(0.5 * std::log2(std::max<double>((double)n, 2.0) / 2.0) + 0.5);
@@ -202,7 +209,7 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     c.k = p->k;
     c.flags = d_flags;
     Launch L{ds.sms, st};
-    KnnTune tune{128, p->k + 16, 0.5f, 1.04f, ds.blocks_per_sm};
+    KnnTune tune{128, p->k + 16, 0.5f, 1.04f, ds.blocks_per_sm[p->k]};
 
     // the array keeps the previous call's contents: clear what starts at zero
     if (cudaMemsetAsync(T.count, 0, T.ncells * sizeof(int32_t), st) != cudaSuccess)

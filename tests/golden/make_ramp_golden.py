@@ -1,6 +1,7 @@
 """Writes tests/golden/color_ramps_ref.npz from the reference's own output image
-(run: python tests/golden/make_ramp_golden.py, in a checkout that holds the
-reference under /root/reference).
+(run: python tests/golden/make_ramp_golden.py PATH/TO/doc/customColorMaps.png,
+the image as it lies in a checkout of the reference; or set
+SPHUGO_COLOR_RAMP_PNG to that path).
 
 doc/customColorMaps.png in the reference is the output of its example
 examples/color-ramp/color-ramp.go: four 20-pixel-wide strips (RainbowRamp,
@@ -16,7 +17,16 @@ import zlib
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = "/root/reference/doc/customColorMaps.png"
+
+def source_png():
+    import sys
+    if len(sys.argv) > 1:
+        return sys.argv[1]
+    path = os.environ.get("SPHUGO_COLOR_RAMP_PNG")
+    if not path:
+        raise SystemExit("usage: make_ramp_golden.py PATH/TO/doc/customColorMaps.png "
+                         "(or set SPHUGO_COLOR_RAMP_PNG)")
+    return path
 
 
 def decode_png_rgb(path):
@@ -65,7 +75,7 @@ def decode_png_rgb(path):
 
 
 def main():
-    img = decode_png_rgb(SRC)
+    img = decode_png_rgb(source_png())
     assert img.shape == (256, 80, 3)
     names = ["rainbow", "para", "heat", "toxic"]
     ramps = {nm: img[255 - np.arange(256), 20 * j + 10].copy() for j, nm in enumerate(names)}

@@ -121,3 +121,20 @@ def test_ensemble_sizes(sphlib):
     assert 5 <= ub.min() and ub.max() <= 50
     lc = np.log(counts)
     assert abs(lc.mean() - 0.5 * (np.log(1000) + np.log(65536))) < 0.3
+
+
+def test_oracle_workloads_equal_the_library_generators(sphlib, oracle):
+    """The benchmark's CPU arms build their inputs with the oracle's copy of
+    the recipes (no GPU library loaded): the arrays must be the library's,
+    bit for bit."""
+    from sphugo_gb300 import ics
+    cases = [(ics.uniform_blast, oracle.uniform_blast, (50_000, 2)),
+             (ics.uniform_blast, oracle.uniform_blast, (7_000, 1005, 1.0, 23.5, 0.1)),
+             (ics.clustered, oracle.clustered, (60_000, 3)),
+             (ics.stress, oracle.stress, (40_000, 4))]
+    for lib_fn, orc_fn, args in cases:
+        for a, b in zip(lib_fn(*args), orc_fn(*args)):
+            assert np.array_equal(a, b), (lib_fn.__name__, args)
+    c1, u1 = ics.ensemble_sizes(256, 5)
+    c2, u2 = oracle.ensemble_sizes(256, 5)
+    assert np.array_equal(c1, c2) and np.array_equal(u1, u2)

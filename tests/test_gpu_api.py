@@ -189,3 +189,53 @@ def test_memory_bytes_counts_the_handle(gpu):
     y = np.ascontiguousarray(x[::-1])
     L.check(gpu.sph_append(a._h, x.size, L.dptr(x), L.dptr(y), None, None, None, None))
     assert a.memory_bytes() > mb
+
+
+def _fnv1a(data: bytes) -> int:
+    h = 1469598103934665603
+    for b in data:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def test_checkpoint_payload_is_checked_before_upload(gpu, tmp_path):
+    """A corrupt payload (hash mismatch) and a payload whose particle ids are
+    not a permutation (hash made to match) are both refused with
+    SPH_ERR_ARG, and the handle keeps its state: the kernels index the
+    caller's order by id, so a bad id must never reach the device."""
+    import struct
+    n = 3000
+    a = _sim(n)
+    a.Step(2)
+    a.Save(tmp_path / "s.ck")
+    data = bytearray((tmp_path / "s.ck").read_bytes())
+    hdr = 72  # header bytes; the payload hash is its last field
+    id_off = hdr + 4 * 16 * n + 3 * 8 * n
+    assert len(data) == hdr + 4 * 16 * n + 3 * 8 * n + 4 * n + 4 * n
+    b = _sim(n)
+    b.Step(1)
+    before = b.state()
+    bad = bytearray(data)
+    bad[hdr + 5] ^= 0x40  # a position bit, hash left as written
+    (tmp_path / "c.ck").write_bytes(bytes(bad))
+    for case, mutate in (("out of range", lambda ids: ids.__setitem__(0, n + 5)),
+                         ("duplicate", lambda ids: ids.__setitem__(0, ids[1])),
+                         ("negative", lambda ids: ids.__setitem__(7, -1))):
+        bad = bytearray(data)
+        ids = np.frombuffer(bytes(bad[id_off:id_off + 4 * n]), np.int32).copy()
+        mutate(ids)
+        bad[id_off:id_off + 4 * n] = ids.tobytes()
+        bad[hdr - 8:hdr] = struct.pack("<Q", _fnv1a(bytes(bad[hdr:])))
+        (tmp_path / f"{case}.ck").write_bytes(bytes(bad))
+    for name in ["c.ck", "out of range.ck", "duplicate.ck", "negative.ck"]:
+        with pytest.raises(L.SphError) as e:
+            b.Load(tmp_path / name)
+        assert e.value.code == L.SPH_ERR_ARG, name
+    assert "hash" in L.last_error() or "permutation" in L.last_error()
+    after = b.state()
+    assert b.CurrentStep == 1
+    for key in before:
+        assert np.array_equal(before[key], after[key]), key
+    # the untouched file still loads
+    b.Load(tmp_path / "s.ck")
+    assert b.CurrentStep == 2

@@ -66,3 +66,16 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
     conf = ics.periodic_config(100, 33, 1e-4)
     p = conf.params()
     assert gpu.sph_density_noalloc(C.byref(p), 1, 1, 100, None, None, None, None, None) == L.SPH_ERR_ARG
+
+
+def test_noalloc_launch_shape_follows_k(gpu):
+    """A call with k = 16 after calls with k = 32 (the search's list shape and
+    launch shape differ by k): still equal to the regular entry points."""
+    n = 3000
+    x, y, *_ = ics.uniform_blast(n, 23)
+    for k in (32, 16, 32):
+        conf = ics.periodic_config(n, k, 1e-4)
+        got = _noalloc(gpu, conf, x, y)
+        want = _regular(conf, x, y)
+        for g, w, name in zip(got, want, ("ids", "dist", "rho", "h")):
+            assert np.array_equal(g, w), (k, name)
