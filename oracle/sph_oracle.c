@@ -378,10 +378,8 @@ static inline int cell_of(const Grid *g, int ax, double v) {
     return (int)t;
 }
 
-static void grid_build(Grid *g, const orc_params *p, const double *x, const double *y, const P *ps, int n, int k) {
-    int gd = (int)floor(sqrt((double)n / (k > 0 ? k : 1)) * 2.0);
-    if (gd < 1) gd = 1;
-    if (gd > 4096) gd = 4096;
+static void grid_build_dim(Grid *g, const orc_params *p, const double *x, const double *y, const P *ps, int n,
+                           int gd) {
     grid_axis(g, 0, p->hor, x, ps, n, gd);
     grid_axis(g, 1, p->vert, y, ps, n, gd);
     size_t nc = (size_t)g->G[0] * g->G[1];
@@ -402,6 +400,41 @@ static void grid_build(Grid *g, const orc_params *p, const double *x, const doub
 }
 
 static void grid_free(Grid *g) { free(g->start); free(g->order); }
+
+/* Uniform grids of every power-of-two resolution from 1 cell per axis up to
+ * the first at or above 4 sqrt(n) (at most 4096) over the same points. A
+ * query searches the finest grid whose cell around it holds at least k/4
+ * points (the coarsest otherwise), so dense and sparse regions both see cells
+ * of a few k points: one uniform grid sized by the mean density degenerates
+ * on strongly clustered data (thousands of points per cell in a dense patch).
+ * The exact result does not depend on the grid: the ring search's stop rule
+ * holds for any cell size. */
+#define PYR_LEVELS 13
+typedef struct {
+    int nl;
+    Grid g[PYR_LEVELS]; /* g[0] finest */
+} Pyramid;
+
+static void pyramid_build(Pyramid *py, const orc_params *p, const double *x, const double *y, const P *ps, int n) {
+    int top = 1;
+    while (top < 4096 && (double)top < 4.0 * sqrt((double)n)) top <<= 1;
+    py->nl = 0;
+    for (int gd = top; gd >= 1 && py->nl < PYR_LEVELS; gd >>= 1) grid_build_dim(&py->g[py->nl++], p, x, y, ps, n, gd);
+}
+
+static void pyramid_free(Pyramid *py) {
+    for (int l = 0; l < py->nl; l++) grid_free(&py->g[l]);
+}
+
+static const Grid *pyramid_pick(const Pyramid *py, double px, double py_, int k) {
+    const int want = k / 4 > 0 ? k / 4 : 1;
+    for (int l = 0; l < py->nl; l++) {
+        const Grid *g = &py->g[l];
+        const int c = cell_of(g, 1, py_) * g->G[0] + cell_of(g, 0, px);
+        if (g->start[c + 1] - g->start[c] >= want) return g;
+    }
+    return &py->g[py->nl - 1];
+}
 
 /* Searches the k best candidates of query i; fills h[0..k) ascending.
  * Returns the number found (< k only if fewer candidates exist). */
@@ -488,9 +521,9 @@ static int knn_standalone(const orc_params *p, const double *x, const double *y,
     double d;
     if (image_range(p->hor, &i0, &i1, &d) || image_range(p->vert, &i0, &i1, &d)) return ORC_ERR_OPEN_MIX;
     if (k <= 0 || n <= k) return ORC_ERR_ARG;
-    Grid g;
-    memset(&g, 0, sizeof g);
-    if (!brute) grid_build(&g, p, x, y, NULL, n, k);
+    Pyramid py;
+    memset(&py, 0, sizeof py);
+    if (!brute) pyramid_build(&py, p, x, y, NULL, n);
     set_threads(p);
 #pragma omp parallel
     {
@@ -498,7 +531,7 @@ static int knn_standalone(const orc_params *p, const double *x, const double *y,
 #pragma omp for schedule(dynamic, 64)
         for (int i = 0; i < n; i++) {
             int cnt = brute ? knn_brute_query(p, x, y, NULL, n, i, h)
-                            : knn_exact_query(&g, p, x, y, NULL, n, i, h);
+                            : knn_exact_query(pyramid_pick(&py, x[i], y[i], k), p, x, y, NULL, n, i, h);
             for (int a = 0; a < k; a++) {
                 ids[(size_t)i * k + a] = a < cnt ? h[a].id : -1;
                 if (d2) d2[(size_t)i * k + a] = a < cnt ? h[a].d2 : INFINITY;
@@ -507,7 +540,7 @@ static int knn_standalone(const orc_params *p, const double *x, const double *y,
         }
         free(h);
     }
-    if (!brute) grid_free(&g);
+    if (!brute) pyramid_free(&py);
     return rc;
 }
 
@@ -565,8 +598,8 @@ static int knn_exact_fill(orc_sim *s) {
     double *y = (double *)malloc((size_t)n * sizeof(double));
     int64_t *ids = (int64_t *)malloc((size_t)n * sizeof(int64_t));
     for (int i = 0; i < n; i++) { x[i] = s->ps[i].x; y[i] = s->ps[i].y; ids[i] = s->ps[i].id; }
-    Grid g;
-    grid_build(&g, &s->p, x, y, NULL, n, k);
+    Pyramid py;
+    pyramid_build(&py, &s->p, x, y, NULL, n);
     int bad = 0;
 #pragma omp parallel reduction(+ : bad)
     {
@@ -574,7 +607,7 @@ static int knn_exact_fill(orc_sim *s) {
 #pragma omp for schedule(dynamic, 64)
         for (int i = 0; i < n; i++) {
             P *p = &s->ps[i];
-            int cnt = knn_exact_query(&g, &s->p, x, y, ids, n, i, h);
+            int cnt = knn_exact_query(pyramid_pick(&py, x[i], y[i], k), &s->p, x, y, ids, n, i, h);
             if (cnt < k) { bad++; continue; }
             for (int a = 0; a < k; a++) {
                 const Cand *c = &h[k - 1 - a]; /* slot 0 = farthest */
@@ -593,7 +626,7 @@ static int knn_exact_fill(orc_sim *s) {
         }
         free(h);
     }
-    grid_free(&g);
+    pyramid_free(&py);
     free(x); free(y); free(ids);
     return bad ? ORC_ERR_SENTINEL : ORC_OK;
 }
@@ -681,8 +714,8 @@ static int calc_forces(orc_sim *s) {
             double *y = (double *)malloc((size_t)n * sizeof(double));
             int64_t *ids = (int64_t *)malloc((size_t)n * sizeof(int64_t));
             for (int i = 0; i < n; i++) { x[i] = s->ps[i].x; y[i] = s->ps[i].y; ids[i] = s->ps[i].id; }
-            Grid g;
-            grid_build(&g, &s->p, x, y, NULL, n, k);
+            Pyramid py;
+            pyramid_build(&py, &s->p, x, y, NULL, n);
             int64_t mm = 0;
 #pragma omp parallel reduction(+ : mm)
             {
@@ -690,13 +723,13 @@ static int calc_forces(orc_sim *s) {
                 int64_t *pairs = (int64_t *)malloc((size_t)k * 2 * sizeof(int64_t));
 #pragma omp for schedule(dynamic, 64)
                 for (int i = 0; i < n; i++) {
-                    knn_exact_query(&g, &s->p, x, y, ids, n, i, h);
+                    knn_exact_query(pyramid_pick(&py, x[i], y[i], k), &s->p, x, y, ids, n, i, h);
                     for (int a = 0; a < k; a++) { pairs[2 * a] = h[a].id; pairs[2 * a + 1] = h[a].img; }
                     if (!same_set(&s->ps[i], s->ps, pairs, k)) mm++;
                 }
                 free(h); free(pairs);
             }
-            grid_free(&g);
+            pyramid_free(&py);
             free(x); free(y); free(ids);
             s->mismatches = mm;
         }

@@ -437,6 +437,17 @@ class Ensemble:
     def Step(self, nsteps: int = 1):
         L.check(L.load().sph_step(self._h, int(nsteps)))
 
+    def CalculateForces(self):
+        """Every simulation's CalculateForces (sim/sph.go:403) on its current
+        state, without integrating."""
+        L.check(L.load().sph_forces(self._h))
+
+    def error_norms(self):
+        """Per-particle normalisers of the mixed form's error statements (FP64 ensembles)."""
+        a, u = np.empty(self.n), np.empty(self.n)
+        L.check(L.load().sph_error_norms(self._h, L.dptr(a), L.dptr(u)))
+        return a, u
+
     def Autotune(self, use_cache: bool = True) -> dict:
         return _autotune(self._h, use_cache)
 
