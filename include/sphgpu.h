@@ -184,12 +184,16 @@ int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms);
 int sph_step_profiled(sph_handle *h, int32_t nsteps, double stage_ms[SPH_NUM_STAGES]);
 /* Kernel launches of one regular step (graph kernel nodes). */
 int32_t sph_kernels_per_step(sph_handle *h);
-/* Neighbour search path (no reference counterpart): 1 (default) = one warp
- * per group of 32 consecutive particles scanning a shared-memory tile of
- * candidate records, with the queries it cannot settle finished by the
- * per-query search; 0 = per-query search for every particle. The neighbour
- * sets and every FP64 result are identical; the mixed form's FP32 sums may
- * differ in the last bits (they follow the list order). */
+/* Neighbour search path (no reference counterpart): tiles of candidate
+ * records in shared memory scanned by one thread per query, the queries they
+ * cannot settle finished by the per-query search. 1 (default) = the default
+ * tile shape for k (block tiles of 8 warps = 256 consecutive particles for
+ * k <= 37, of 4 warps for k <= 80, else one tile per warp); 4 or 8 = block
+ * tiles of that many warps; 2 = one tile per warp (32 particles); 0 =
+ * per-query search for every particle. The neighbour sets and every FP64
+ * result are identical on every path; the mixed form's FP32 sums may differ
+ * in the last bits (they follow the list order). SPH_ERR_ARG for a shape
+ * that k does not allow. */
 int sph_set_search(sph_handle *h, int32_t tiles);
 /* Queries of the last force evaluation and how many of them the group-tile
  * search left to the per-query search (all of them with tiles off). */

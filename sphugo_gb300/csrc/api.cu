@@ -45,6 +45,13 @@ const double kMonahanPref = 0x1.5d3b3e3583243p+3;
 const double kWendFPref = 0x1.1d34a60108f72p+1;
 const double kWendDFPref = 0x1.1d34a60108f72p+2;
 
+// Tiles shared by eight warps for lists of up to 40 entries (k <= 37), by
+// four for longer lists up to k = 80; one tile per warp beyond.
+int default_block_warps(int k) {
+    const int need = (3 * k) / 2 + 8;
+    return need <= 64 ? 8 : need <= 128 ? 4 : 0;
+}
+
 int auto_level(int64_t n) {
     // about one to four particles per finest cell
     double l = std::floor(0.5 * std::log2(std::max<double>((double)n, 2.0) / 2.0) + 0.5);
@@ -449,6 +456,7 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     h->tune.blocks_per_sm = std::max(1, knn_occupancy_blocks(h->tune.block, h->tune.cap, h->mode));
     h->tune.tile = 1;
     h->tune.tile_blocks_per_sm = std::max(1, knn_tile_occupancy_blocks((int)k, h->mode));
+    h->tune.block_warps = default_block_warps((int)k);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return bail(fail(SPH_ERR_CUDA, cudaGetErrorString(e)));
     *out = h;
@@ -514,7 +522,7 @@ std::string tune_cache_path() {
 
 struct TuneChoice {
     float theta = 0.5f, hgrow = 1.04f;
-    int delta = 0, tile = 1;
+    int delta = 0, tile = 1, block = 8;
     double ms = 0.0;
 };
 
@@ -531,7 +539,7 @@ bool tune_cache_get(const std::string &key, TuneChoice *c) {
     std::string line;
     bool found = false;
     while (std::getline(f, line)) {
-        if (line.rfind("sphgpu-tune-v2 " + key + " ", 0) != 0) continue;
+        if (line.rfind("sphgpu-tune-v3 " + key + " ", 0) != 0) continue;
         std::istringstream in(line.substr(16 + key.size()));
         std::string tok;
         while (in >> tok) {
@@ -542,6 +550,7 @@ bool tune_cache_get(const std::string &key, TuneChoice *c) {
             else if (k == "hgrow") c->hgrow = std::stof(v);
             else if (k == "delta") c->delta = std::stoi(v);
             else if (k == "tile") c->tile = std::stoi(v);
+            else if (k == "block") c->block = std::stoi(v);
             else if (k == "ms") c->ms = std::stod(v);
         }
         found = true;  // the last matching line wins
@@ -555,8 +564,8 @@ void tune_cache_put(const std::string &key, const TuneChoice &c) {
     std::filesystem::create_directories(std::filesystem::path(path).parent_path(), ec);
     std::ofstream f(path, std::ios::app);
     if (!f) return;
-    f << "sphgpu-tune-v2 " << key << " theta=" << c.theta << " hgrow=" << c.hgrow << " delta=" << c.delta
-      << " tile=" << c.tile << " ms=" << c.ms << "\n";
+    f << "sphgpu-tune-v3 " << key << " theta=" << c.theta << " hgrow=" << c.hgrow << " delta=" << c.delta
+      << " tile=" << c.tile << " block=" << c.block << " ms=" << c.ms << "\n";
 }
 
 }  // namespace
@@ -1033,10 +1042,17 @@ int sph_render(sph_handle *h, int32_t width, int32_t height, uint8_t *rgba) {
 }
 
 int sph_set_search(sph_handle *h, int32_t tiles) {
-    if (!h || (tiles != 0 && tiles != 1)) return fail(SPH_ERR_ARG, "bad handle or search path");
+    if (!h || (tiles != 0 && tiles != 1 && tiles != 2 && tiles != 4 && tiles != 8))
+        return fail(SPH_ERR_ARG, "bad handle or search path");
     Guard g(h);
-    if (h->tune.tile != tiles) {
-        h->tune.tile = tiles;
+    const int bdef = default_block_warps(h->k);
+    if ((tiles == 4 || tiles == 8) && tiles > bdef)
+        return fail(SPH_ERR_ARG, "no block tiles of that many warps for this k");
+    const int tile = tiles ? 1 : 0;
+    const int block = tiles == 1 ? bdef : tiles == 2 ? 0 : tiles == 0 ? h->tune.block_warps : tiles;
+    if (h->tune.tile != tile || h->tune.block_warps != block) {
+        h->tune.tile = tile;
+        h->tune.block_warps = block;
         destroy_graphs(h);
     }
     return SPH_OK;
@@ -1103,17 +1119,22 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
     int trials = 0;
     const int reps = std::max(1, std::min(3, (int)(150.0 / std::max(ms0, 1e-3))));
     if (!cached) {
-        // (search path, cell side / radius): group tiles (theta then only shapes
-        // the deferred queries' search) or the per-query search
-        const int tiles[] = {1, 0, 0, 0};
-        const float thetas[] = {0.5f, 0.35f, 0.5f, 0.7f};
+        // (search path, tile shape, cell side / radius): block tiles of eight
+        // or four warps, one tile per warp (theta then only shapes the
+        // deferred queries' search), or the per-query search
+        const int tiles[] = {1, 1, 1, 0, 0, 0};
+        const int blocks[] = {8, 4, 0, 0, 0, 0};
+        const float thetas[] = {0.5f, 0.5f, 0.5f, 0.35f, 0.5f, 0.7f};
         const float hgrows[] = {1.02f, 1.04f, 1.08f};
+        const int bdef = default_block_warps(h->k);
         best.ms = 1e300;
         const int dmax = (cv < 0.6) ? 1 : 2;  // clustered data: dense regions want finer cells
         for (int delta = -1; delta <= dmax; delta++) {
             if ((rc = apply_levels(h, delta))) continue;
-            for (int v = 0; v < 4; v++) {
+            for (int v = 0; v < 6; v++) {
+                if (blocks[v] > bdef) continue;  // no block kernel with that many warps for this k
                 h->tune.tile = tiles[v];
+                h->tune.block_warps = blocks[v];
                 h->tune.theta = thetas[v];
                 h->tune.hgrow = 1.04f;
                 destroy_graphs(h);
@@ -1124,6 +1145,7 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
                     best.ms = ms;
                     best.theta = thetas[v];
                     best.tile = tiles[v];
+                    best.block = blocks[v];
                     best.delta = delta;
                     best.hgrow = 1.04f;
                 }
@@ -1132,6 +1154,7 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
         if ((rc = apply_levels(h, best.delta))) return rc;
         h->tune.theta = best.theta;
         h->tune.tile = best.tile;
+        h->tune.block_warps = best.block;
         for (float hg : hgrows) {
             if (hg == 1.04f) continue;
             h->tune.hgrow = hg;
@@ -1147,6 +1170,7 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
     h->tune.theta = best.theta;
     h->tune.hgrow = best.hgrow;
     h->tune.tile = best.tile;
+    h->tune.block_warps = best.block;
     if ((rc = apply_levels(h, best.delta))) return rc;
     // back to the uploaded state
     launch_scatter_state(h->ctx(), h->launch(), h->A, d, d + n, d + 2 * n, d + 3 * n, d + 4 * n, nullptr, nullptr,
@@ -1158,7 +1182,7 @@ int sph_autotune(sph_handle *h, int32_t use_cache, char *report, int32_t report_
         std::ostringstream o;
         o << "{\"key\": \"" << key << "\", \"cached\": " << (cached ? "true" : "false") << ", \"trials\": " << trials
           << ", \"theta\": " << best.theta << ", \"hgrow\": " << best.hgrow << ", \"level_delta\": " << best.delta
-          << ", \"tiles\": " << best.tile
+          << ", \"tiles\": " << best.tile << ", \"block_warps\": " << best.block
           << ", \"ms_per_eval\": " << best.ms << ", \"ms_default\": " << ms0 << ", \"h_cv\": " << cv
           << ", \"cache\": \"" << tune_cache_path() << "\"}";
         strncpy(report, o.str().c_str(), (size_t)report_len - 1);
@@ -1179,7 +1203,7 @@ struct CkptHeader {
     int32_t nsims, k, step, level_delta;
     uint64_t params_hash;
     float theta, hgrow;  // search shape (the mixed form's sums follow its visiting order)
-    int32_t tile, pad;   // search path (group tiles or per query)
+    int32_t tile, block_warps;  // search path (group tiles or per query) and tile shape
     uint64_t payload_hash;  // FNV-1a of the state arrays as stored
 };
 
@@ -1231,6 +1255,8 @@ int check_checkpoint(const sph_handle *h, const CkptHeader &hd, const std::vecto
     for (int64_t i = 0; i < n; i++)
         if (!(hprev[i] >= 0.f && hprev[i] < 3.0e38f)) return fail(SPH_ERR_ARG, "checkpoint smoothing lengths invalid");
     if (!(hd.theta > 0.f && hd.theta < 64.f) || !(hd.hgrow > 0.f && hd.hgrow < 64.f) || (hd.tile != 0 && hd.tile != 1) ||
+        (hd.block_warps != 0 && hd.block_warps != 4 && hd.block_warps != 8) ||
+        hd.block_warps > default_block_warps(h->k) ||
         hd.level_delta < -kMaxLevel || hd.level_delta > kMaxLevel || hd.step < 0)
         return fail(SPH_ERR_ARG, "checkpoint search settings out of range");
     return SPH_OK;
@@ -1255,6 +1281,7 @@ int sph_save(sph_handle *h, const char *path) {
     hd.theta = h->tune.theta;
     hd.hgrow = h->tune.hgrow;
     hd.tile = h->tune.tile;
+    hd.block_warps = h->tune.block_warps;
     const std::vector<ArrayRef> arrays = state_arrays(h);
     std::vector<std::vector<char>> bufs(arrays.size());
     uint64_t ph = 1469598103934665603ull;
@@ -1296,10 +1323,12 @@ int sph_load(sph_handle *h, const char *path) {
     }
     if ((rc = check_checkpoint(h, hd, bufs))) return rc;
     if (hd.level_delta != h->level_delta && (rc = apply_levels(h, hd.level_delta))) return rc;
-    if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow || hd.tile != h->tune.tile) {
+    if (hd.theta != h->tune.theta || hd.hgrow != h->tune.hgrow || hd.tile != h->tune.tile ||
+        hd.block_warps != h->tune.block_warps) {
         h->tune.theta = hd.theta;
         h->tune.hgrow = hd.hgrow;
         h->tune.tile = hd.tile;
+        h->tune.block_warps = hd.block_warps;
         destroy_graphs(h);
     }
     for (size_t i = 0; i < arrays.size(); i++)

@@ -216,6 +216,7 @@ struct KnnTune {
     int blocks_per_sm; // resident blocks per SM at this block size / capacity
     int tile;          // 1: group tiles first, per-query search for the deferred queries
     int tile_blocks_per_sm;
+    int block_warps;   // tiles shared by the warps of a block (4 or 8 warps; 0: one tile per warp)
 };
 void knn_init_attrs();
 void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D,

@@ -26,34 +26,12 @@
 // FP64 squared distance, density (sim/sph.go:306-323),
 // c = sqrt(gamma (gamma-1) u_pred) and c^2/(gamma rho).
 // The neighbour set and its order are identical in every arithmetic form.
-#include "physics.cuh"
+#include "knn_shared.cuh"
 
 #include <algorithm>
 #include <cstddef>
 
 namespace sphgpu {
-
-struct KnnArgs {
-    Ctx c;
-    PArrays B;
-    Derived D;
-    const int32_t *start;
-    float theta, hgrow;
-    int use_defer;  // per-query kernel: walk the deferred list instead of every particle
-};
-
-// |d2_f32 - d2_ref| <= kEpsRel * d2 + eps_abs(R): the float-pair difference
-// carries ~2^-23 relative error, the two float products ~2^-24 each, and the
-// reference's own rounding of (p + offset) adds ~2^-53 L absolute per axis.
-constexpr float kEpsRel = 9.5367431640625e-7f;  // 2^-20 (about 8x the bound)
-
-__device__ __forceinline__ float eps_of(float d2, float abs_term) { return kEpsRel * d2 + abs_term; }
-
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
 
 template <int NR>
 struct ListShape {
@@ -558,46 +536,6 @@ constexpr int kTileRows = 64;
 constexpr int kTileBox = 1024;
 constexpr int kTileCells = 511;  // cells whose record offsets a tile keeps (lane-rectangle scans)
 
-// Batcher's odd-even merge sort (K. E. Batcher, "Sorting networks and their
-// applications", 1968) of NS keys in registers, ascending: the network for the
-// next power of two with every comparator that touches a position >= NS left
-// out (those positions would hold +infinity and never move).
-template <int NS>
-struct OddEvenSort {
-    uint32_t (&v)[NS];
-    __device__ __forceinline__ void ce(int i, int j) {
-        if (j < NS) {
-            const uint32_t lo = min(v[i], v[j]);
-            v[j] = max(v[i], v[j]);
-            v[i] = lo;
-        }
-    }
-    template <int LO, int N, int R>
-    __device__ __forceinline__ void merge() {
-        constexpr int M = 2 * R;
-        if constexpr (M < N) {
-            merge<LO, N, M>();
-            merge<LO + R, N, M>();
-#pragma unroll
-            for (int i = LO + R; i + R < LO + N; i += M) ce(i, i + R);
-        } else {
-            ce(LO, LO + R);
-        }
-    }
-    template <int LO, int N>
-    __device__ __forceinline__ void sort() {
-        if constexpr (N > 1 && LO < NS) {
-            sort<LO, N / 2>();
-            sort<LO + N / 2, N / 2>();
-            merge<LO, N, 1>();
-        }
-    }
-    __device__ __forceinline__ void run() {
-        constexpr int P2 = NS <= 32 ? 32 : NS <= 64 ? 64 : 128;
-        sort<0, P2>();
-    }
-};
-
 template <int NR>
 struct TileSmem {
     // per-query list capacity: k + 3 or more (k <= 37 for NR = 2); lists
@@ -622,23 +560,6 @@ static_assert(offsetof(TileSmem<1>, list) % 16 == 0 && offsetof(TileSmem<2>, lis
                   offsetof(TileSmem<4>, list) % 16 == 0 && offsetof(TileSmem<8>, list) % 16 == 0 &&
                   sizeof(TileSmem<2>) % 16 == 0 && offsetof(TileSmem<2>, rect) % 16 == 0,
               "tile shared-memory members must keep their alignment");
-
-// d2 in units of R^2 / 2^23 rounded to the nearest integer, clamped to 23
-// bits, without a conversion instruction: for 0 <= d2 qs < 2^23 the FMA
-// d2 qs + 2^23 lands in [2^23, 2^24), where the float's mantissa is the
-// integer itself.
-__device__ __forceinline__ uint32_t key23(float d2, float qs) {
-    return min(__float_as_uint(__fmaf_rn(d2, qs, 8388608.f)) - 0x4B000000u, 8388607u);
-}
-
-__device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t q, int lane) {
-    const uint32_t bal = __ballot_sync(0xffffffffu, mine);
-    if (!bal) return;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(a.D.ndefer, __popc(bal));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (mine) a.D.defer[base + __popc(bal & lanemask_lt())] = (int32_t)q;
-}
 
 // Register budgets: the FP64 forms with lists of <= 40 entries get 128
 // registers (four blocks per SM, which shared memory allows); the mixed form
@@ -1204,6 +1125,7 @@ void knn_init_attrs() {
     knn_attrs_mode<MODE_EXACT64>();
     knn_attrs_mode<MODE_FAST64>();
     knn_attrs_mode<MODE_MIXED>();
+    knn_block_init_attrs();
 }
 
 template <int MODE, int NR>
@@ -1247,11 +1169,13 @@ static void launch_knn_nr(const KnnArgs &args, const Launch &L, const KnnTune &t
     if (tune.tile && args.D.defer) {
         // group tiles, then the per-query kernel over the deferred queries
         cudaMemsetAsync(args.D.ndefer, 0, sizeof(int32_t), L.stream);
-        const int64_t groups = (args.c.n + 31) / 32;
-        const int64_t tneed = (groups + kTileWarps - 1) / kTileWarps;
-        const int tgrid = (int)std::max<int64_t>(
-            1, std::min<int64_t>(tneed, (int64_t)L.sms * std::max(tune.tile_blocks_per_sm, 1)));
-        k_knn_tile<MODE, NR><<<tgrid, kTileWarps * 32, kTileWarps * sizeof(TileSmem<NR>), L.stream>>>(args);
+        if (!(tune.block_warps > 0 && launch_knn_block(args, L, MODE, NR, tune.block_warps))) {
+            const int64_t groups = (args.c.n + 31) / 32;
+            const int64_t tneed = (groups + kTileWarps - 1) / kTileWarps;
+            const int tgrid = (int)std::max<int64_t>(
+                1, std::min<int64_t>(tneed, (int64_t)L.sms * std::max(tune.tile_blocks_per_sm, 1)));
+            k_knn_tile<MODE, NR><<<tgrid, kTileWarps * 32, kTileWarps * sizeof(TileSmem<NR>), L.stream>>>(args);
+        }
         KnnArgs d = args;
         d.use_defer = 1;
         k_knn<MODE, NR><<<std::max(resident, 1), kKnnBlock, smem, L.stream>>>(d);

@@ -139,8 +139,10 @@ class SphConfig:
 
 
 
-def _set_search(h, tiles: bool):
-    L.check(L.load().sph_set_search(h, 1 if tiles else 0))
+def _set_search(h, tiles):
+    """True / 1: tiles of the default shape; 2: one tile per warp; 4 or 8:
+    block tiles of that many warps; False / 0: per-query search."""
+    L.check(L.load().sph_set_search(h, int(tiles)))
 
 
 def _search_stats(h) -> tuple:
@@ -290,8 +292,10 @@ class Simulation:
         """Picks the neighbour search's launch shape for this workload (before the first step)."""
         return _autotune(self._h, use_cache)
 
-    def SetSearch(self, tiles: bool):
-        """Group-tile neighbour search (default) or per-query search; same neighbour sets."""
+    def SetSearch(self, tiles=True):
+        """Neighbour search path: True / 1 tiles of the default shape, 8 or 4
+        block tiles of that many warps, 2 one tile per warp, False / 0 the
+        per-query search; every path returns the same neighbour sets."""
         _set_search(self._h, tiles)
 
     def search_stats(self) -> tuple:
@@ -451,7 +455,7 @@ class Ensemble:
     def Autotune(self, use_cache: bool = True) -> dict:
         return _autotune(self._h, use_cache)
 
-    def SetSearch(self, tiles: bool):
+    def SetSearch(self, tiles=True):
         _set_search(self._h, tiles)
 
     def search_stats(self) -> tuple:
