@@ -150,6 +150,10 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
     uint32_t *cellw = reinterpret_cast<uint32_t *>(sm.rec);  // build phase: (first particle << 4) | image
     uint32_t (*mylist)[32] = sm.u.list[w];
 
+    for (int r = tid; r < kRowCap; r += NT) {
+        sm.rx0[r] = INT_MAX;
+        sm.rx1[r] = INT_MIN;
+    }
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t q0 = tile * Q;
         const int64_t q = q0 + tid;
@@ -232,14 +236,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
             const int shift = level - sh, Gl = 1 << shift;
             // a box wider than one period would hold a particle twice
             tile_ok = tile_ok && (BX1 - BX0 + 1) <= Gl && ny <= Gl;
-            if (tile_ok) {
-                for (int r = tid; r < ny; r += NT) {
-                    sm.rx0[r] = INT_MAX;
-                    sm.rx1[r] = INT_MIN;
-                }
-            }
-            __syncthreads();
-            // ---- row hulls
+            // ---- row hulls (the rows were reset at the end of the previous pass)
             if (tile_ok && valid) {
                 const int lx0 = x0 >> sh, lx1 = x1 >> sh;
                 for (int vy = y0 >> sh; vy <= (y1 >> sh); vy++) {
@@ -337,7 +334,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                 }
                 total = all;
                 int run = wbase + inc - sum;
-                __syncthreads();  // every thread has read the warp sums
+                // (the warp sums are next written in the next pass, after its barriers)
                 if (tile_ok && total <= TCAP) {
 #pragma unroll
                     for (int i = 0; i < CPT; i++) {
@@ -421,13 +418,20 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                     const int base = sm.rpre[rr] - sm.rx0[rr];
                     int t = cx0 <= cx1 ? sm.cstart[base + cx0] : 0;
                     const int e = cx0 <= cx1 ? sm.cstart[base + cx1 + 1] : 0;
-                    for (; t < e; t++) {
-                        const float2 cc = sm.rec[t];
-                        const float dx = cc.x - rqx, dy = cc.y - rqy;
-                        const float d2 = __fmaf_rn(dx, dx, dy * dy);
-                        const bool pass = d2 <= R2 && t != myself;
-                        mylist[min(cnt, LCAP)][lane] = (key_of<KB>(d2, qs) << SB) | (uint32_t)t;
-                        cnt += pass ? 1 : 0;
+                    // four records per round, their loads issued together (the
+                    // round's tail repeats the row's last record and never passes)
+                    for (; t < e; t += 4) {
+                        float2 cc[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) cc[u] = sm.rec[min(t + u, e - 1)];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const float dx = cc[u].x - rqx, dy = cc[u].y - rqy;
+                            const float d2 = __fmaf_rn(dx, dx, dy * dy);
+                            const bool pass = d2 <= R2 && t + u != myself && t + u < e;
+                            mylist[min(cnt, LCAP)][lane] = (key_of<KB>(d2, qs) << SB) | (uint32_t)(t + u);
+                            cnt += pass ? 1 : 0;
+                        }
                     }
                 }
             }
@@ -488,15 +492,25 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                 int32_t *out = a.D.nbr + q * k;
                 float *o2 = a.D.d2f + q * k;
                 int o = 0;
-                for (int e = 0; e < cnt; e++) {
-                    const uint32_t v = mylist[e][lane];
-                    if (v <= kth) {
-                        const uint32_t slot = v & BS::SMASK;
-                        const float2 cc = sm.rec[slot];
-                        const float dx = cc.x - rqx, dy = cc.y - rqy;
-                        const int at = v == kth ? k - 1 : o++;
-                        out[at] = (int32_t)sm.code[slot];
-                        o2[at] = __fmaf_rn(dx, dx, dy * dy);
+                for (int e0 = 0; e0 < cnt; e0 += 4) {
+                    uint32_t v[4], cd[4];
+                    float2 cc[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) v[u] = e0 + u < cnt ? mylist[e0 + u][lane] : 0xffffffffu;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const uint32_t slot = min(v[u] & BS::SMASK, (uint32_t)(TCAP - 1));
+                        cc[u] = sm.rec[slot];
+                        cd[u] = sm.code[slot];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (v[u] <= kth) {
+                            const float dx = cc[u].x - rqx, dy = cc[u].y - rqy;
+                            const int at = v[u] == kth ? k - 1 : o++;
+                            out[at] = (int32_t)cd[u];
+                            o2[at] = __fmaf_rn(dx, dx, dy * dy);
+                        }
                     }
                 }
             } else if (ok) {
@@ -507,7 +521,11 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                 }
             }
             defer_lanes(a, valid && !ok, q, lane);
-            __syncthreads();  // the tile is reused by the next pass
+            __syncthreads();  // every thread is done with the rows and the tile
+            for (int r = tid; r < kRowCap; r += NT) {  // rows reset for the next pass
+                sm.rx0[r] = INT_MAX;
+                sm.rx1[r] = INT_MIN;
+            }
         }
     }
 }

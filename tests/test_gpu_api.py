@@ -74,7 +74,8 @@ def test_autotune_keeps_results_and_caches(gpu, tmp_path, monkeypatch, precision
     c = _sim(12_000, precision)
     rep2 = c.Autotune(use_cache=True)
     assert rep2["cached"] is True and rep2["theta"] == rep["theta"] and rep2["level_delta"] == rep["level_delta"]
-    assert (tmp_path / "tune.txt").read_text().count("sphgpu-tune-v2") == 1
+    assert rep2["block_warps"] == rep["block_warps"] and rep2["tiles"] == rep["tiles"]
+    assert (tmp_path / "tune.txt").read_text().count("sphgpu-tune-v3") == 1
 
 
 @pytest.mark.parametrize("precision", ["Exact", "Mixed"])
