@@ -276,11 +276,11 @@ def library_inputs(kind, n, seed):
     return {"clustered": ics.clustered, "stress": ics.stress, "blast": ics.uniform_blast}[kind](n, seed)
 
 
-def make_sim(kind, n, k, dt, seed, form, tune=True):
+def make_sim(kind, n, k, dt, seed, form, tune=True, level=0):
     """A workload's simulation, autotuned (the tuner caches its choice)."""
     from sphugo_gb300 import ics
     from sphugo_gb300 import sim as S
-    sim = S.Simulation(ics.periodic_config(n, k, dt, form), *library_inputs(kind, n, seed))
+    sim = S.Simulation(ics.periodic_config(n, k, dt, form, grid_level=level), *library_inputs(kind, n, seed))
     sim.tune_report = sim.Autotune() if tune else None
     return sim
 
@@ -493,6 +493,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="exact", choices=["exact", "fast", "mixed"],
                     help="arithmetic form of the headline run (profiling only; default exact)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed form's line (profiling only)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="no autotuning: default search shape at the binning level --level (profiling only)")
+    ap.add_argument("--level", type=int, default=0, help="binning level with --no-tune (0: automatic)")
     args = ap.parse_args()
     dist = Dist()
     try:
@@ -535,7 +539,8 @@ def run_ours(args, dist):
     slot_peak = fp64_pk.value / 2 * 1e3  # G FP64 FMA issue slots per second
 
     form = {"exact": "Exact", "fast": "Fast", "mixed": "Mixed"}[args.form]
-    sim = make_sim(HEAD_KIND, n, HEAD_K, HEAD_DT, HEAD_SEED + 1000 * dist.rank, form)
+    sim = make_sim(HEAD_KIND, n, HEAD_K, HEAD_DT, HEAD_SEED + 1000 * dist.rank, form, tune=not args.no_tune,
+                   level=args.level if args.no_tune else 0)
     tune_report = sim.tune_report
     sim.Step(W)
     kernels = int(lib.sph_kernels_per_step(sim._h))
@@ -555,7 +560,7 @@ def run_ours(args, dist):
     hbm_bytes = sim.memory_bytes()
     lo_frac, visc_frac = pair_statistics(sim, HEAD_DT / 2)
     work = algorithmic(HEAD_K, div_cost.value, sqrt_cost.value, lo_frac, visc_frac)
-    level = auto_level(n) + int((tune_report or {}).get("level_delta", 0))
+    level = args.level if args.no_tune and args.level else auto_level(n) + int((tune_report or {}).get("level_delta", 0))
     roof = stage_rooflines(stages, work, n, form, level, slot_peak, hbm)
     dom = max(stages, key=stages.get)
     d = roof[dom]
@@ -576,7 +581,7 @@ def run_ours(args, dist):
     sim.close()
 
     mixed = None
-    if dist.rank == 0 and form == "Exact":
+    if dist.rank == 0 and form == "Exact" and not args.no_mixed:
         sm = make_sim(HEAD_KIND, n, HEAD_K, HEAD_DT, HEAD_SEED, "Mixed")
         sm.Step(W)
         t = timed(sm, K)
