@@ -486,9 +486,38 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
             ok = ok && (cnt == k || nxt - tau > 2.f * (kEpsRel * nxt + ea));
             if (MODE == MODE_MIXED) ok = ok && (k == 1 || tau - prv > 2.f * et);
             else ok = ok && order_ok;
-            if (ok && MODE == MODE_MIXED) {
+            // Outputs go out four entries per store (each list row is 16-byte
+            // aligned: q k 4 bytes with k a multiple of four).
+            bool stored = false;
+            if constexpr (SEL32) {
+                if (ok && k == 32) {
+                    // the selected set straight from registers, the farthest last
+                    // (it fixes h): kth and the entry in arr[31] trade places
+                    int4 *out4 = reinterpret_cast<int4 *>(a.D.nbr + q * 32);
+                    float4 *o24 = reinterpret_cast<float4 *>(a.D.d2f + q * 32);
+#pragma unroll
+                    for (int c = 0; c < 8; c++) {
+                        uint32_t cd[4];
+                        float dd[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const int i = 4 * c + u;
+                            const uint32_t v = i == 31 ? kth : (arr[i] == kth ? arr[31] : arr[i]);
+                            const uint32_t slot = v & BS::SMASK;
+                            const float2 cc = sm.rec[slot];
+                            const float dx = cc.x - rqx, dy = cc.y - rqy;
+                            cd[u] = sm.code[slot];
+                            dd[u] = __fmaf_rn(dx, dx, dy * dy);
+                        }
+                        out4[c] = make_int4((int)cd[0], (int)cd[1], (int)cd[2], (int)cd[3]);
+                        o24[c] = make_float4(dd[0], dd[1], dd[2], dd[3]);
+                    }
+                    stored = true;
+                }
+            }
+            if (ok && !stored && MODE == MODE_MIXED) {
                 // the set with the farthest last (it fixes h), the rest in tile
-                // (cell) order, which keeps the force pass's gathers close
+                // (cell) order
                 int32_t *out = a.D.nbr + q * k;
                 float *o2 = a.D.d2f + q * k;
                 int o = 0;
@@ -513,11 +542,23 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                         }
                     }
                 }
-            } else if (ok) {
+            } else if (ok && MODE != MODE_MIXED) {
+                // sorted, nearest first
                 int32_t *out = a.D.nbr + q * k;
+                if ((k & 3) == 0) {
+                    int4 *out4 = reinterpret_cast<int4 *>(out);
 #pragma unroll
-                for (int i = 0; i < A; i++) {
-                    if (i < k) out[i] = (int32_t)sm.code[arr[i] & BS::SMASK];
+                    for (int c = 0; c < A / 4; c++) {
+                        if (4 * c < k)
+                            out4[c] = make_int4((int)sm.code[arr[4 * c] & BS::SMASK], (int)sm.code[arr[4 * c + 1] & BS::SMASK],
+                                                (int)sm.code[arr[4 * c + 2] & BS::SMASK],
+                                                (int)sm.code[arr[4 * c + 3] & BS::SMASK]);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < A; i++) {
+                        if (i < k) out[i] = (int32_t)sm.code[arr[i] & BS::SMASK];
+                    }
                 }
             }
             defer_lanes(a, valid && !ok, q, lane);
