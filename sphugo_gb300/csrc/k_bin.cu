@@ -152,15 +152,28 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &
     return r;
 }
 
+// A thread's eight consecutive cells (32-byte aligned) as two 16-byte loads;
+// cells past the end read as empty.
+__device__ __forceinline__ void load_counts(const Tables &T, int64_t base, int (&v)[kScanItems]) {
+    if (base + kScanItems <= T.ncells) {
+        const int4 a = *reinterpret_cast<const int4 *>(T.count + base);
+        const int4 b = *reinterpret_cast<const int4 *>(T.count + base + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++) v[j] = base + j < T.ncells ? T.count[base + j] : 0;
+    }
+}
+
 __global__ void k_scan_tiles(Tables T) {
     __shared__ int ws[32];
     int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int v[kScanItems];
+    load_counts(T, base, v);
     int sum = 0;
 #pragma unroll
-    for (int j = 0; j < kScanItems; j++) {
-        int64_t idx = base + j;
-        if (idx < T.ncells) sum += T.count[idx];
-    }
+    for (int j = 0; j < kScanItems; j++) sum += v[j];
     int total;
     block_exclusive_scan(sum, ws, total);
     if (threadIdx.x == 0) T.partial[blockIdx.x] = total;
@@ -188,20 +201,25 @@ __global__ void k_scan_final(Tables T) {
     __shared__ int ws[32];
     int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
     int v[kScanItems];
+    load_counts(T, base, v);
     int sum = 0;
 #pragma unroll
-    for (int j = 0; j < kScanItems; j++) {
-        int64_t idx = base + j;
-        v[j] = idx < T.ncells ? T.count[idx] : 0;
-        sum += v[j];
-    }
+    for (int j = 0; j < kScanItems; j++) sum += v[j];
     int total;
     int ex = block_exclusive_scan(sum, ws, total) + T.partial[blockIdx.x];
+    int st[kScanItems];
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
-        int64_t idx = base + j;
-        if (idx < T.ncells) T.start[idx] = ex;
+        st[j] = ex;
         ex += v[j];
+    }
+    if (base + kScanItems <= T.ncells) {
+        *reinterpret_cast<int4 *>(T.start + base) = make_int4(st[0], st[1], st[2], st[3]);
+        *reinterpret_cast<int4 *>(T.start + base + 4) = make_int4(st[4], st[5], st[6], st[7]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanItems; j++)
+            if (base + j < T.ncells) T.start[base + j] = st[j];
     }
 }
 
