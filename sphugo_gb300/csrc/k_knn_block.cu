@@ -29,9 +29,9 @@
 //      3 eps inside R, the (k+1)-th more than 2 eps beyond it, and in the FP64
 //      forms every neighbour more than 2 eps from the next.
 // The FP64 forms sort each list with Batcher's network (order needed); the
-// mixed form at k = 32 only selects the eight largest of forty (five sorted
-// groups of eight merged pairwise: 175 comparators instead of 610) since it
-// needs the set, the k-th and its neighbours in rank.
+// mixed form at k = 16, 32 and 64 only selects the k smallest of its 24, 40
+// or 96 list entries (TopGroups below) since it needs the set, the k-th and
+// its neighbours in rank.
 #include "knn_shared.cuh"
 
 #include <algorithm>
@@ -61,39 +61,43 @@ __device__ __forceinline__ uint32_t key_of(float d2, float qs) {
     return min(__float_as_uint(__fmaf_rn(d2, qs, 8388608.f)) - 0x4B000000u, (1u << KB) - 1u);
 }
 
-// The 8 largest of 40 keys (Batcher's 19-comparator sorter on five groups of
-// eight, then pairwise merges: the top eight of two ascending groups are the
-// larger of each pair (a[i], b[7-i]), a bitonic sequence that a 12-comparator
-// half-cleaner network sorts). Afterwards v[32..39] hold the eight largest in
-// ascending order and v[0..31] the 32 smallest, unordered.
-struct Top8Of40 {
-    uint32_t (&v)[40];
+// The G largest of A keys (A a multiple of G, G a power of two): A / G
+// groups of G, each sorted by Batcher's odd-even merge network, then merged
+// pairwise: the top G of two ascending groups a, b are the larger of each pair
+// (a[i], b[G-1-i]), a bitonic sequence that a half-cleaner network sorts.
+// Afterwards v[A-G..A-1] hold the G largest in ascending order and
+// v[0..A-G-1] the others, unordered. A = 40, G = 8 takes 175 comparators
+// (five 19-comparator sorts, four merges of 8 + 12) against the full sort's
+// 610; A = 96, G = 32 takes 797 against 2112.
+template <int A, int G>
+struct TopGroups {
+    uint32_t (&v)[A];
     __device__ __forceinline__ void ce(int i, int j) {
         const uint32_t lo = min(v[i], v[j]);
         v[j] = max(v[i], v[j]);
         v[i] = lo;
     }
-    __device__ __forceinline__ void sort8(int b) {
-        ce(b + 0, b + 1); ce(b + 2, b + 3); ce(b + 4, b + 5); ce(b + 6, b + 7);
-        ce(b + 0, b + 2); ce(b + 1, b + 3); ce(b + 4, b + 6); ce(b + 5, b + 7);
-        ce(b + 1, b + 2); ce(b + 5, b + 6);
-        ce(b + 0, b + 4); ce(b + 1, b + 5); ce(b + 2, b + 6); ce(b + 3, b + 7);
-        ce(b + 2, b + 4); ce(b + 3, b + 5);
-        ce(b + 1, b + 2); ce(b + 3, b + 4); ce(b + 5, b + 6);
-    }
-    __device__ __forceinline__ void bitonic8(int b) {
-        ce(b + 0, b + 4); ce(b + 1, b + 5); ce(b + 2, b + 6); ce(b + 3, b + 7);
-        ce(b + 0, b + 2); ce(b + 1, b + 3); ce(b + 4, b + 6); ce(b + 5, b + 7);
-        ce(b + 0, b + 1); ce(b + 2, b + 3); ce(b + 4, b + 5); ce(b + 6, b + 7);
+    template <int GI>
+    __device__ __forceinline__ void sort_groups() {
+        if constexpr (GI < A / G) {
+            OddEvenSort<A>{v}.template sort<GI * G, G>();
+            sort_groups<GI + 1>();
+        }
     }
     __device__ __forceinline__ void run() {
+        static_assert(A % G == 0 && (G & (G - 1)) == 0, "groups of a power-of-two size");
+        sort_groups<0>();
 #pragma unroll
-        for (int g = 0; g < 5; g++) sort8(8 * g);
+        for (int g = 0; g + 1 < A / G; g++) {
 #pragma unroll
-        for (int g = 0; g < 4; g++) {
+            for (int i = 0; i < G; i++) ce(g * G + i, (g + 2) * G - 1 - i);
+            const int b = (g + 1) * G;
 #pragma unroll
-            for (int i = 0; i < 8; i++) ce(8 * g + i, 8 * g + 15 - i);
-            bitonic8(8 * g + 8);
+            for (int st = G / 2; st >= 1; st >>= 1) {
+#pragma unroll
+                for (int i = 0; i < G; i++)
+                    if ((i & st) == 0) ce(b + i, b + i + st);
+            }
         }
     }
 };
@@ -138,7 +142,10 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
     constexpr int Q = BS::Q, TCAP = BS::TCAP, SB = BS::SB, KB = BS::KB, CCAP = BS::CCAP, LCAP = BS::LCAP;
     constexpr int NT = WARPS * 32;
     constexpr uint32_t FULL = 0xffffffffu;
-    constexpr bool SEL32 = MODE == MODE_MIXED && NR == 2;  // the top-8 selection applies when k == 32
+    // the mixed form selects (rather than sorts) when k leaves a power-of-two
+    // remainder of the list: k = 16 of 24, 32 of 40, 64 of 96
+    constexpr bool SEL = MODE == MODE_MIXED && NR <= 4;
+    constexpr int KSEL = NR == 1 ? 16 : NR == 2 ? 32 : 64;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BS &sm = *reinterpret_cast<BS *>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -462,17 +469,17 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                     }
                 }
             };
-            if constexpr (SEL32) {
-                if (k == 32) {
-                    if (ok) Top8Of40{arr}.run();
-                    // the k-th smallest is the largest of v[0..31], the (k-1)-th
-                    // the second largest, the (k+1)-th the smallest of the top eight
+            if constexpr (SEL) {
+                if (k == KSEL) {
+                    if (ok) TopGroups<A, A - KSEL>{arr}.run();
+                    // the k-th smallest is the largest of v[0..k-1], the (k-1)-th
+                    // the second largest, the (k+1)-th the smallest of the top group
 #pragma unroll
-                    for (int i = 0; i < 32; i++) {
+                    for (int i = 0; i < KSEL; i++) {
                         kprv = max(kprv, min(kth, arr[i]));
                         kth = max(kth, arr[i]);
                     }
-                    knx = arr[32];
+                    knx = arr[KSEL];
                 } else {
                     sorted_path();
                 }
@@ -489,20 +496,20 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
             // Outputs go out four entries per store (each list row is 16-byte
             // aligned: q k 4 bytes with k a multiple of four).
             bool stored = false;
-            if constexpr (SEL32) {
-                if (ok && k == 32) {
+            if constexpr (SEL) {
+                if (ok && k == KSEL) {
                     // the selected set straight from registers, the farthest last
-                    // (it fixes h): kth and the entry in arr[31] trade places
-                    int4 *out4 = reinterpret_cast<int4 *>(a.D.nbr + q * 32);
-                    float4 *o24 = reinterpret_cast<float4 *>(a.D.d2f + q * 32);
+                    // (it fixes h): kth and the entry in arr[k-1] trade places
+                    int4 *out4 = reinterpret_cast<int4 *>(a.D.nbr + q * KSEL);
+                    float4 *o24 = reinterpret_cast<float4 *>(a.D.d2f + q * KSEL);
 #pragma unroll
-                    for (int c = 0; c < 8; c++) {
+                    for (int c = 0; c < KSEL / 4; c++) {
                         uint32_t cd[4];
                         float dd[4];
 #pragma unroll
                         for (int u = 0; u < 4; u++) {
                             const int i = 4 * c + u;
-                            const uint32_t v = i == 31 ? kth : (arr[i] == kth ? arr[31] : arr[i]);
+                            const uint32_t v = i == KSEL - 1 ? kth : (arr[i] == kth ? arr[KSEL - 1] : arr[i]);
                             const uint32_t slot = v & BS::SMASK;
                             const float2 cc = sm.rec[slot];
                             const float dx = cc.x - rqx, dy = cc.y - rqy;
