@@ -202,8 +202,8 @@ int sph_search_stats(sph_handle *h, int64_t *queries, int64_t *deferred);
  * the first step) it times forces-only evaluations over a small grid of the
  * neighbour search's shape (search path and tile shape: block tiles of 8 or
  * 4 warps, one tile per warp, or the per-query search; cell side / search
- * radius factor, radius-guess growth, automatic binning level -1..+1, or
- * -1..+2 for clustered data), keeps the fastest, restores the
+ * radius factor, automatic binning level -1..+1, or -1..+2 for clustered
+ * data), keeps the fastest, restores the
  * uploaded state and caches the choice per (particle count in half octaves,
  * k, arithmetic form, single/ensemble, distribution class from the spread of
  * smoothing lengths) in the text file named by SPHGPU_TUNE_CACHE (default

@@ -166,6 +166,8 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     SimDev *d_sims = cv.take<SimDev>(1);
     int64_t *d_offs = cv.take<int64_t>(2);
     unsigned *d_flags = cv.take<unsigned>(1);
+    if ((size_t)(cv.p - ds.ptr) > kScratchBytes)
+        return nfail(SPH_ERR_ARG, "sph_density_noalloc: internal scratch layout exceeds the static array");
 
     // constants of this call: the automatic binning level for n, capped to
     // the scratch's cell table (p->grid_level is not used)
