@@ -299,7 +299,7 @@ void enqueue_eval(sph_handle *h, int pred, bool integrate, bool events = false) 
     mark(3);
     launch_knn(c, L, h->B, h->D, h->T, h->mode, h->tune);
     mark(4);
-    launch_density(c, L, h->B, h->D, h->mode);
+    launch_density(c, L, h->B, h->D, h->mode, &h->tune);
     mark(5);
     launch_force(c, L, h->B, h->A, h->D, h->mode, integrate);
     mark(6);

@@ -221,7 +221,10 @@ struct KnnTune {
 void knn_init_attrs();
 void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D,
                 const Tables &T, int mode, const KnnTune &tune);
-void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode);
+// tune: the search's shape (NULL: a search without tiles); when the block
+// tiles computed the settled queries' densities, only the deferred are done
+void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode,
+                    const KnnTune *tune);
 void force_init_attrs(int k);
 void launch_force(const Ctx &c, const Launch &L, const PArrays &B, const PArrays &A,
                   const Derived &D, int mode, bool integrate);

@@ -937,19 +937,6 @@ __global__ void __launch_bounds__(kTileWarps * 32, (MODE == MODE_MIXED || NR > 2
 }
 
 // ---------------------------------------------------------------- density
-// the reference's squared distance to the neighbour image a list code names
-__device__ __forceinline__ double nbr_d2(const SimDev &S, const PArrays &B, double2 P, uint32_t code) {
-    const double2 Q = B.pos[code >> kCodeShift];
-    if ((code & 15u) == 4u) {
-        // no offset: p + 0 = p (and -0 + 0 = +0 squares to the same value)
-        const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
-        return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-    }
-    double ox, oy;
-    img_shift(S, code & 15u, ox, oy);
-    return dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
-}
-
 // five resident blocks (48 registers): the FP64 forms' first loop waits on the
 // neighbour gathers, and more resident warps hide them (2.06 -> 2.02 ms at N = 1M)
 template <int MODE>
@@ -957,8 +944,12 @@ __global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
     const int k = a.c.k;
     const PArrays &B = a.B;
     unsigned fl = 0;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < a.c.n;
-         q += (int64_t)gridDim.x * blockDim.x) {
+    // all particles, or (use_defer) only the queries the block tiles left to
+    // the per-query search: the tiles computed the others' densities
+    const int64_t nq = a.use_defer ? (int64_t)*a.D.ndefer : a.c.n;
+    for (int64_t qi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; qi < nq;
+         qi += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = a.use_defer ? (int64_t)a.D.defer[qi] : qi;
         const int s = sim_of(a.c, q);
         const SimDev &S = a.c.sims[s];
         const double gamma = S.gamma;
@@ -1161,6 +1152,12 @@ int knn_tile_occupancy_blocks(int k, int mode) {
     return pick(occ_tile<MODE_MIXED, 1>, occ_tile<MODE_MIXED, 2>, occ_tile<MODE_MIXED, 4>, occ_tile<MODE_MIXED, 8>);
 }
 
+bool knn_fuses_density(int k, int mode, const KnnTune &tune) {
+    const int nr = list_regs(k);
+    return mode == MODE_MIXED && tune.tile && tune.block_warps > 0 && nr <= 4 &&
+           k == (nr == 1 ? 16 : nr == 2 ? 32 : 64);
+}
+
 template <int MODE, int NR>
 static void launch_knn_nr(const KnnArgs &args, const Launch &L, const KnnTune &tune) {
     const int wpb = kKnnBlock / 32;
@@ -1212,16 +1209,19 @@ void launch_knn(const Ctx &c, const Launch &L, const PArrays &B, const Derived &
     a.theta = tune.theta;
     a.hgrow = tune.hgrow;
     a.use_defer = 0;
+    a.fuse_density = knn_fuses_density(c.k, mode, tune) ? 1 : 0;
     if (mode == MODE_EXACT64) run_knn<MODE_EXACT64>(a, L, tune);
     else if (mode == MODE_FAST64) run_knn<MODE_FAST64>(a, L, tune);
     else run_knn<MODE_MIXED>(a, L, tune);
 }
 
-void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode) {
+void launch_density(const Ctx &c, const Launch &L, const PArrays &B, const Derived &D, int mode,
+                    const KnnTune *tune) {
     KnnArgs a{};
     a.c = c;
     a.B = B;
     a.D = D;
+    a.use_defer = tune && D.defer && knn_fuses_density(c.k, mode, *tune) ? 1 : 0;
     if (mode == MODE_EXACT64) run_density<MODE_EXACT64>(a, L);
     else if (mode == MODE_FAST64) run_density<MODE_FAST64>(a, L);
     else run_density<MODE_MIXED>(a, L);

@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
     float4 *staging = sm.u.staging;
     uint32_t *cellw = reinterpret_cast<uint32_t *>(sm.rec);  // build phase: (first particle << 4) | image
     uint32_t (*mylist)[32] = sm.u.list[w];
+    unsigned fl = 0;  // device error flags of this thread's queries
 
     for (int r = tid; r < kRowCap; r += NT) {
         sm.rx0[r] = INT_MAX;
@@ -502,8 +503,22 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                     // (it fixes h): kth and the entry in arr[k-1] trade places
                     int4 *out4 = reinterpret_cast<int4 *>(a.D.nbr + q * KSEL);
                     float4 *o24 = reinterpret_cast<float4 *>(a.D.d2f + q * KSEL);
+                    // With the density fused (k_density's mixed form for this query):
+                    // h from the farthest neighbour's FP64 squared distance in the
+                    // reference's rounding, then the FP32 kernel sum over the
+                    // squared distances written here, which then need not be stored
+                    const bool fuse = a.fuse_density != 0;
+                    double hq = 0.0;
+                    float inv_hf = 0.f;
+                    if (fuse) {
+                        const double dk2 = nbr_d2(S, B, B.pos[q], sm.code[kth & BS::SMASK]);
+                        if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
+                        hq = __dsqrt_rn(dk2);
+                        inv_hf = 1.f / __double2float_rn(hq);
+                    }
+                    KahanF acc;  // farthest first, the order of k_density's sum
 #pragma unroll
-                    for (int c = 0; c < KSEL / 4; c++) {
+                    for (int c = KSEL / 4 - 1; c >= 0; c--) {
                         uint32_t cd[4];
                         float dd[4];
 #pragma unroll
@@ -517,7 +532,22 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                             dd[u] = __fmaf_rn(dx, dx, dy * dy);
                         }
                         out4[c] = make_int4((int)cd[0], (int)cd[1], (int)cd[2], (int)cd[3]);
-                        o24[c] = make_float4(dd[0], dd[1], dd[2], dd[3]);
+                        if (fuse) {
+#pragma unroll
+                            for (int u = 3; u >= 0; u--) acc.add(kf_f32(S.kernel, fminf(sqrtf(dd[u]) * inv_hf, 1.f)));
+                        } else {
+                            o24[c] = make_float4(dd[0], dd[1], dd[2], dd[3]);
+                        }
+                    }
+                    if (fuse) {
+                        const float hf = __double2float_rn(hq);
+                        const float rhof = S.ffm * (inv_hf * inv_hf) * acc.value_f();
+                        const float csf = sqrtf(S.fgg1 * __double2float_rn(B.up[q]));
+                        const float ctf = csf * csf / (S.fgamma * rhof);
+                        a.D.rho[q] = rhof;
+                        a.D.c[q] = csf;
+                        a.D.h[q] = hq;
+                        a.D.derf[q] = make_float4(csf, rhof, hf, ctf);
                     }
                     stored = true;
                 }
@@ -576,6 +606,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
             }
         }
     }
+    if (fl) atomicOr(a.c.flags, fl);
 }
 
 // ------------------------------------------------------------------ launch

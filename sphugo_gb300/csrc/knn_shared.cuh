@@ -13,7 +13,8 @@ struct KnnArgs {
     Derived D;
     const int32_t *start;
     float theta, hgrow;
-    int use_defer;  // per-query kernel: walk the deferred list instead of every particle
+    int use_defer;  // per-query kernel / density: walk the deferred list instead of every particle
+    int fuse_density;  // mixed block tiles: each settled query's density computed with its list
 };
 
 // |d2_f32 - d2_ref| <= kEpsRel * d2 + eps_abs(R): the float-pair difference
@@ -86,9 +87,25 @@ __device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t
     if (mine) a.D.defer[base + __popc(bal & lanemask_lt())] = (int32_t)q;
 }
 
+// the reference's squared distance to the neighbour image a list code names
+__device__ __forceinline__ double nbr_d2(const SimDev &S, const PArrays &B, double2 P, uint32_t code) {
+    const double2 Q = B.pos[code >> kCodeShift];
+    if ((code & 15u) == 4u) {
+        // no offset: p + 0 = p (and -0 + 0 = +0 squares to the same value)
+        const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
+        return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    }
+    double ox, oy;
+    img_shift(S, code & 15u, ox, oy);
+    return dist_sq_ref(P.x, P.y, ox, oy, Q.x, Q.y);
+}
+
 // block-tile search (k_knn_block.cu): false when no block kernel serves the
 // list shape nr (the warp tiles do then)
 bool launch_knn_block(const KnnArgs &args, const Launch &L, int mode, int nr, int warps);
+// whether the block tiles compute the mixed form's densities of the queries
+// they settle (the density pass then covers only the deferred queries)
+bool knn_fuses_density(int k, int mode, const KnnTune &tune);
 void knn_block_init_attrs();
 
 }  // namespace sphgpu

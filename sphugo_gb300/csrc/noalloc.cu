@@ -228,7 +228,7 @@ extern "C" int sph_density_noalloc(const sph_params *p, const double *x, const d
     launch_stable(c, L, T);
     launch_permute(c, L, A, B, T, PRED_INIT, false);
     launch_knn(c, L, B, D, T, MODE_EXACT64, tune);
-    launch_density(c, L, B, D, MODE_EXACT64);
+    launch_density(c, L, B, D, MODE_EXACT64, nullptr);
     if (nbr_ids || nbr_dist) launch_gather_neighbours(c, L, B, B, D, nbr_ids, nbr_dist, nullptr, true);
     if (rho || hsml) launch_gather_derived(c, L, B, D, rho, nullptr, hsml);
     cudaError_t e = cudaGetLastError();
