@@ -43,7 +43,7 @@ EXPORTS = [
     "sph_config_start_count", "sph_config_spawn", "sph_point_source_spawn",
     "sph_step_timed", "sph_step_profiled", "sph_kernels_per_step", "sph_set_search", "sph_search_stats",
     "sph_probe_peaks", "sph_append", "sph_set_draw_keys", "sph_render", "sph_para_ramp",
-    "sph_density_noalloc", "sph_autotune", "sph_save", "sph_load", "sph_selftest_division",
+    "sph_density_noalloc", "sph_autotune", "sph_save", "sph_load", "sph_selftest_division", "sph_selftest_fp64emu",
 ]
 NOALLOC_MAX_N = 8192
 NOALLOC_MAX_K = 32
@@ -156,6 +156,7 @@ def load() -> C.CDLL:
     L.sph_autotune.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
     L.sph_save.argtypes = [vp, C.c_char_p]
     L.sph_selftest_division.argtypes = [C.c_int64, C.c_uint64, i64p]
+    L.sph_selftest_fp64emu.argtypes = [C.c_int64, C.c_uint64, i64p]
     L.sph_load.argtypes = [vp, C.c_char_p]
     L.sph_density_noalloc.argtypes = [C.POINTER(SphParams), vp, vp, C.c_int32, vp, vp, vp, vp, vp]
     _lib = L

@@ -18,7 +18,7 @@ LIB = os.path.join(PKG, "libsphgpu.so")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["k_bin.cu", "k_knn.cu", "k_knn_block.cu", "k_force.cu", "k_util.cu", "k_render.cu", "api.cu", "noalloc.cu"]
 CPP_SOURCES = ["ic.cpp", "config.cpp"]
-HEADERS = ["common.cuh", "physics.cuh", "knn_shared.cuh"]
+HEADERS = ["common.cuh", "physics.cuh", "knn_shared.cuh", "fp64emu.cuh"]
 
 
 def nvcc() -> str:

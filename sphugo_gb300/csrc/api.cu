@@ -1079,6 +1079,14 @@ int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches) {
     return SPH_OK;
 }
 
+int sph_selftest_fp64emu(int64_t n, uint64_t seed, int64_t *mismatches) {
+    if (!mismatches || n < 0) return fail(SPH_ERR_ARG, "bad argument");
+    long long m = 0;
+    if (emu_selftest(n, seed, &m)) return fail(SPH_ERR_CUDA, "fp64 emulation self-check failed to run");
+    *mismatches = m;
+    return SPH_OK;
+}
+
 int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {

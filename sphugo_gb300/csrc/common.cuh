@@ -247,6 +247,7 @@ int knn_occupancy_blocks(int block, int cap, int mode);
 int knn_tile_occupancy_blocks(int k, int mode);
 int probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, double *sqrt_cost);
 int div_selftest(int64_t n, uint64_t seed, long long *mismatches);
+int emu_selftest(int64_t n, uint64_t seed, long long *mismatches);
 // message returned by sph_last_error() on this thread
 void set_last_error(const std::string &msg);
 

@@ -159,7 +159,7 @@ __device__ __forceinline__ void pair_geom(const SimDev &S, const PArrays &B, uin
         rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
         raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
     }
-    dot = __dadd_rn(__dmul_rn(vabx, rabx), __dmul_rn(vaby, raby));
+    dot = __dadd_rn(emu_mul(vabx, rabx), emu_mul(vaby, raby));
 }
 
 template <int MODE>
@@ -314,9 +314,9 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                     const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
                     // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
                     const double yd = __drcp_rn(d);
-                    ax = __dadd_rn(ax, div_rn_recip(__dmul_rn(__dmul_rn(rabx, sum3), drk), d, yd));
-                    ay = __dadd_rn(ay, div_rn_recip(__dmul_rn(__dmul_rn(raby, sum3), drk), d, yd));
-                    ed = __dadd_rn(ed, __dmul_rn(dot, drk));
+                    ax = __dadd_rn(ax, div_rn_recip(emu_mul(emu_mul(rabx, sum3), drk), d, yd));
+                    ay = __dadd_rn(ay, div_rn_recip(emu_mul(emu_mul(raby, sum3), drk), d, yd));
+                    ed = __dadd_rn(ed, emu_mul(dot, drk));
                 });
                 const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
                 axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);

@@ -988,15 +988,15 @@ __global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
                 for (int e = k - 1; e >= s_lo; e--) {  // q >= 0.5
                     const double x = dist[e].y;
                     const double a1 = __dsub_rn(1.0, x);
-                    const double a2 = __dmul_rn(a1, a1);
-                    acc = __dadd_rn(acc, div3_rn(__dmul_rn(a2, a1)));
+                    const double a2 = emu_mul(a1, a1);
+                    acc = __dadd_rn(acc, div3_rn(emu_mul(a2, a1)));
                     dist[e].y = -a2;
                 }
                 for (int e = s_lo - 1; e >= 0; e--) {  // q < 0.5
                     const double x = dist[e].y;
-                    const double qq = __dmul_rn(x, x);
-                    acc = __dadd_rn(acc, __dadd_rn(__dsub_rn(__dmul_rn(qq, x), qq), 1.0 / 6.0));
-                    dist[e].y = __dsub_rn(__dmul_rn(__dmul_rn(3.0, x), x), __dmul_rn(2.0, x));
+                    const double qq = emu_mul(x, x);
+                    acc = __dadd_rn(acc, __dadd_rn(__dsub_rn(emu_mul(qq, x), qq), 1.0 / 6.0));
+                    dist[e].y = __dsub_rn(emu_mul(emu_mul(3.0, x), x), emu_mul(2.0, x));
                 }
             }
             rho = __ddiv_rn(__dmul_rn(__dmul_rn(S.fpref, S.mass), acc), __dmul_rn(h, h));

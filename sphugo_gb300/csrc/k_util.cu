@@ -2,6 +2,7 @@
 // cell order kept on the device, neighbour-list export in the reference's
 // layout, and the diagnostics of sim/sph.go:441-463.
 #include "physics.cuh"
+#include "fp64emu.cuh"
 
 namespace sphgpu {
 
@@ -335,6 +336,93 @@ __global__ void k_div_selftest(int64_t n, uint64_t seed, unsigned long long *bad
         if (div3_rn(a) != __ddiv_rn(a, 3.0)) nb++;
     }
     if (nb) atomicAdd(bad, nb);
+}
+
+// ---- self-check of the integer-pipe binary64 operations against the hardware
+// One operand pair per index, from one of six classes: raw random bits (every
+// exponent, zeros, subnormals, infinities, NaNs); normals of nearby
+// exponents; short significands (exact ties in products and sums); exponents
+// at the ends of the range (overflow, underflow, subnormal results); near
+// cancellation (y = -x with its low bits changed); specials against normals.
+__device__ __forceinline__ double emu_operand(uint64_t r, uint32_t cls, uint32_t e0) {
+    uint64_t frac = r & kEmuFrac;
+    uint32_t ex = e0;
+    switch (cls) {
+    case 0: return emu_double(r);
+    case 2: frac &= 0x000FFFFFC0000000ull; break;  // 22 significant fraction bits
+    default: break;
+    }
+    return emu_double((r & kEmuSign) | ((uint64_t)ex << 52) | frac);
+}
+
+__device__ __forceinline__ bool emu_same(double x, double y) {
+    return emu_bits(x) == emu_bits(y) || (x != x && y != y);
+}
+
+__global__ void k_emu_selftest(int64_t n, uint64_t seed, unsigned long long *bad) {
+    unsigned long long nb = 0;
+    const double specials[8] = {0.0, -0.0, __longlong_as_double(1ll), __longlong_as_double(0x000FFFFFFFFFFFFFll),
+                                __longlong_as_double(0x7FF0000000000000ll), __longlong_as_double((long long)0xFFF0000000000000ull),
+                                __longlong_as_double(0x7FF8000000000000ll), 0x1p-1022};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t r1 = mix64(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(3 * i + 1));
+        const uint64_t r2 = mix64(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(3 * i + 2));
+        const uint64_t r3 = mix64(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(3 * i + 3));
+        const uint32_t cls = (uint32_t)(i % 6);
+        double x, y;
+        if (cls == 0) {
+            x = emu_double(r1);
+            y = emu_double(r2);
+        } else if (cls == 1 || cls == 2) {
+            // exponents 1000-1047 apart by 0 .. 63 (both classes): alignment
+            // shifts of every length, carries, cancellation
+            const uint32_t ex = 1000u + (uint32_t)(r3 % 48u);
+            const uint32_t ey = 1000u + (uint32_t)((r3 >> 8) % 48u) + ((r3 >> 16) & 1u ? (uint32_t)((r3 >> 20) % 16u) : 0u);
+            x = emu_operand(r1, cls, ex);
+            y = emu_operand(r2, cls, ey);
+        } else if (cls == 3) {
+            // the ends of the range: products and sums near overflow and underflow
+            const uint32_t lo = (uint32_t)(r3 & 1u);
+            const uint32_t ex = lo ? 1u + (uint32_t)((r3 >> 1) % 64u) : 1983u + (uint32_t)((r3 >> 1) % 64u);
+            const uint32_t ey = (r3 >> 8) & 1u ? 1023u + (uint32_t)((r3 >> 9) % 64u) - 32u
+                                               : (lo ? 1u + (uint32_t)((r3 >> 9) % 64u) : 1983u + (uint32_t)((r3 >> 9) % 64u));
+            x = emu_operand(r1, 1, ex);
+            y = emu_operand(r2, 1, ey);
+        } else if (cls == 4) {
+            // near cancellation: y = -x with its low 0 .. 52 bits replaced, or
+            // one exponent step away
+            x = emu_operand(r1, 1, 900u + (uint32_t)(r3 % 256u));
+            const uint32_t nbits = (uint32_t)((r3 >> 8) % 53u);
+            const uint64_t mask = nbits ? ((1ull << nbits) - 1ull) : 0ull;
+            uint64_t yb = (emu_bits(x) & ~mask) | (r2 & mask);
+            if ((r3 >> 16) & 1u) yb += ((r3 >> 17) & 1u) ? (1ull << 52) : (uint64_t)-(int64_t)(1ull << 52);
+            y = emu_double(yb ^ kEmuSign);
+        } else {
+            x = specials[r3 & 7u];
+            y = emu_operand(r2, 1, 1u + (uint32_t)((r3 >> 3) % 2046u));
+            if ((r3 >> 16) & 1u) { const double t = x; x = y; y = t; }
+        }
+        if (!emu_same(emu_mul(x, y), __dmul_rn(x, y))) nb++;
+        if (!emu_same(emu_add(x, y), __dadd_rn(x, y))) nb++;
+        if (!emu_same(emu_sub(x, y), __dsub_rn(x, y))) nb++;
+    }
+    if (nb) atomicAdd(bad, nb);
+}
+
+int emu_selftest(int64_t n, uint64_t seed, long long *mismatches) {
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof *d) != cudaSuccess) return -1;
+    cudaMemset(d, 0, sizeof *d);
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_emu_selftest<<<sms * 8, 256>>>(n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return -1;
+    *mismatches = (long long)h;
+    return 0;
 }
 
 int div_selftest(int64_t n, uint64_t seed, long long *mismatches) {

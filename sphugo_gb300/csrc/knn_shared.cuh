@@ -93,7 +93,7 @@ __device__ __forceinline__ double nbr_d2(const SimDev &S, const PArrays &B, doub
     if ((code & 15u) == 4u) {
         // no offset: p + 0 = p (and -0 + 0 = +0 squares to the same value)
         const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
-        return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        return __dadd_rn(emu_mul(dx, dx), emu_mul(dy, dy));
     }
     double ox, oy;
     img_shift(S, code & 15u, ox, oy);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "fp64emu.cuh"
 
 namespace sphgpu {
 
@@ -20,7 +21,7 @@ namespace sphgpu {
 // RN(a/3). Valid for every finite a without underflow in r.
 __device__ __forceinline__ double div3_rn(double a) {
     const double y = 0x1.5555555555555p-2;  // RN(1/3)
-    const double q0 = __dmul_rn(a, y);
+    const double q0 = emu_mul(a, y);
     const double r = __fma_rn(-3.0, q0, a);
     return __fma_rn(r, y, q0);
 }
@@ -31,7 +32,7 @@ __device__ __forceinline__ double div3_rn(double a) {
 // faithful) makes RN(q1 + r1 y) the correctly rounded quotient. No
 // overflow/underflow for the operands used here (distances and their ratios).
 __device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
-    const double q0 = __dmul_rn(a, y);
+    const double q0 = emu_mul(a, y);
     const double r0 = __fma_rn(-b, q0, a);
     const double q1 = __fma_rn(r0, y, q0);
     const double r1 = __fma_rn(-b, q1, a);
@@ -160,15 +161,15 @@ __device__ __forceinline__ double dist_sq_ref(double px, double py, double ox, d
                                               double qx, double qy) {
     double dx = __dsub_rn(__dadd_rn(px, ox), qx);
     double dy = __dsub_rn(__dadd_rn(py, oy), qy);
-    return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    return __dadd_rn(emu_mul(dx, dx), emu_mul(dy, dy));
 }
 
 // image code (i+1)*3+(j+1) -> shift (i*dX, j*dY), as float64(i)*deltaX in
-// sim/nearest-neighbour.go:59
+// sim/nearest-neighbour.go:59 (i = +-1: the product is exactly +-deltaX)
 __device__ __forceinline__ void img_shift(const SimDev &S, uint32_t img, double &ox, double &oy) {
     int ia = (int)(img / 3u) - 1, ib = (int)(img % 3u) - 1;
-    ox = ia ? __dmul_rn((double)ia, S.dimg[0]) : 0.0;
-    oy = ib ? __dmul_rn((double)ib, S.dimg[1]) : 0.0;
+    ox = ia ? (ia > 0 ? S.dimg[0] : -S.dimg[0]) : 0.0;
+    oy = ib ? (ib > 0 ? S.dimg[1] : -S.dimg[1]) : 0.0;
 }
 
 }  // namespace sphgpu

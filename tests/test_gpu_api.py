@@ -115,6 +115,18 @@ def test_division_sequences_are_correctly_rounded(gpu):
     assert bad.value == 0
 
 
+def test_integer_pipe_fp64_operations_match_the_hardware(gpu):
+    """The FP64 kernels compute some multiplications, additions and
+    subtractions with integer instructions; each must return the hardware
+    instruction's bits. 3 x 2^31 results over random bit patterns, nearby and
+    extreme exponents, exact ties, near cancellation and special values."""
+    bad = C.c_int64(-1)
+    L.check(gpu.sph_selftest_fp64emu(1 << 31, 2024, C.byref(bad)))
+    assert bad.value == 0
+    L.check(gpu.sph_selftest_fp64emu(1 << 28, 7, C.byref(bad)))
+    assert bad.value == 0
+
+
 @pytest.mark.parametrize("precision,k", [("Exact", 32), ("Mixed", 32), ("Exact", 16), ("Mixed", 16),
                                          ("Exact", 64), ("Mixed", 64)])
 def test_group_tiles_match_per_query_search(gpu, precision, k):
