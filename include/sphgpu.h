@@ -248,13 +248,14 @@ int sph_density_noalloc(const sph_params *p, const double *x, const double *y, i
 int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches);
 
 /* Self-check (no reference counterpart): runs the library's binary64
- * multiplication, addition and subtraction computed with integer
- * instructions (which the FP64 kernels use beside the hardware FP64 unit)
- * against the hardware instructions on 3 n results from n seeded operand
- * pairs (random bits, nearby and extreme exponents, exact ties, near
- * cancellation, zeros, subnormals, infinities and NaNs) and reports the
- * number of results that differ in any bit (NaN against NaN counts as
- * equal; 0 expected). */
+ * multiplication, addition, subtraction, division and square root computed
+ * with integer instructions (which the FP64 kernels use beside the hardware
+ * FP64 unit) against the hardware instructions on 5 n results from n seeded
+ * operand pairs (random bits, nearby and extreme exponents, exact ties, near
+ * cancellation, perfect squares and their neighbours, quotients next to
+ * rounding boundaries, zeros, subnormals,
+ * infinities and NaNs) and reports the number of results that differ in any
+ * bit (NaN against NaN counts as equal; 0 expected). */
 int sph_selftest_fp64emu(int64_t n, uint64_t seed, int64_t *mismatches);
 
 /* Page-locks (pins) caller memory so that transfers from / to it run at

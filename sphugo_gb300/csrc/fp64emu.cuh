@@ -1,6 +1,6 @@
-// fp64emu.cuh -- binary64 multiplication, addition and subtraction, rounded
-// to nearest with ties to even (IEEE 754-2019, 4.3.1), computed with integer
-// instructions.
+// fp64emu.cuh -- binary64 multiplication, addition, subtraction, division
+// and square root, rounded to nearest with ties to even (IEEE 754-2019,
+// 4.3.1), computed with integer instructions (and FP32 seeds).
 //
 // GB300 issues two FP64 lanes per SM per clock: one warp-wide FP64
 // instruction holds a sub-partition's FP64 unit for about 64 cycles, while
@@ -41,6 +41,8 @@ namespace sphgpu {
 static __device__ __noinline__ double emu_native_mul(double x, double y) { return __dmul_rn(x, y); }
 static __device__ __noinline__ double emu_native_add(double x, double y) { return __dadd_rn(x, y); }
 static __device__ __noinline__ double emu_native_sub(double x, double y) { return __dsub_rn(x, y); }
+static __device__ __noinline__ double emu_native_sqrt(double x) { return __dsqrt_rn(x); }
+static __device__ __noinline__ double emu_native_div(double x, double y) { return __ddiv_rn(x, y); }
 #else
 __device__ __forceinline__ double emu_native_mul(double x, double y) {
     double r;
@@ -55,6 +57,16 @@ __device__ __forceinline__ double emu_native_add(double x, double y) {
 __device__ __forceinline__ double emu_native_sub(double x, double y) {
     double r;
     asm volatile("sub.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
+    return r;
+}
+__device__ __forceinline__ double emu_native_sqrt(double x) {
+    double r;
+    asm volatile("sqrt.rn.f64 %0, %1;" : "=d"(r) : "d"(x));
+    return r;
+}
+__device__ __forceinline__ double emu_native_div(double x, double y) {
+    double r;
+    asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
     return r;
 }
 #endif
@@ -143,7 +155,156 @@ __device__ __forceinline__ double emu_addsub(double x, double y) {
     return emu_double(r);
 }
 
+// S^2 for S < 2^54 as two 64-bit words
+__device__ __forceinline__ void emu_sq_wide(uint64_t S, uint64_t &hi, uint64_t &lo) {
+    const uint32_t sh = (uint32_t)(S >> 32), sl = (uint32_t)S;
+    const uint64_t ll = (uint64_t)sl * sl, mid = ((uint64_t)sl * sh) << 1, hh = (uint64_t)sh * sh;
+    lo = ll + (mid << 32);
+    hi = hh + (mid >> 32) + (lo < ll ? 1ull : 0ull);
+}
+
+// RN(sqrt(x)). With x = M0 2^p (M0 the significand, shifted left once when
+// p is odd) the result's significand is RN(sqrt(M)) for the integer
+// M = M0 2^52 in [2^104, 2^106): S0 from the FP32 reciprocal square root
+// y0 ~ 1/sqrt(M0 2^-52) (about 21 good bits), two Newton corrections
+// S += (M - S^2) y0 / (2 sqrt(M)) evaluated on 32-bit windows of the exact
+// 128-bit residual (the error falls from ~2^32 to ~2^12 to below 0.51), then
+// the exact remainder r = M - S^2 makes S the floor (0 <= r <= 2S) and
+// decides the rounding: up iff r > S (sqrt(M) > S + 1/2; never a tie for an
+// integer M). The method is Newton's iteration for the square root with an
+// exact integer remainder test, e.g. R. Brent and P. Zimmermann, "Modern
+// Computer Arithmetic", 2010, section 1.5.1.
+__device__ __forceinline__ double emu_sqrt(double x) {
+    const uint64_t a = emu_bits(x);
+    const uint32_t ah = (uint32_t)(a >> 32);
+    const uint32_t e = ah >> 20;  // with the sign bit: > 2046 for negative x
+    const uint32_t odd = ~e & 1u;  // the unbiased exponent e - 1075 is odd
+    const uint64_t M0 = ((a & kEmuFrac) | kEmuHidden) << odd;  // [2^52, 2^54)
+    const uint64_t Mhi = M0 >> 12, Mlo = M0 << 52;  // M = M0 2^52
+    const float uf = __uint2float_rn((uint32_t)(M0 >> 30)) * 0x1p-22f;  // M0 2^-52 in [1, 4), 24 bits
+    const float y0 = rsqrtf(uf);
+    uint64_t S = (uint64_t)__float2uint_rn(uf * y0 * 0x1p23f) << 29;  // ~ sqrt(M)
+    uint64_t hi, lo;
+    // first correction: |M - S^2| < 2^86, read as bits 56 .. 87
+    emu_sq_wide(S, hi, lo);
+    {
+        const uint64_t rlo = Mlo - lo, rhi = Mhi - hi - (Mlo < lo ? 1ull : 0ull);
+        const int32_t w = (int32_t)__funnelshift_r((uint32_t)(rlo >> 32), (uint32_t)rhi, 24);
+        // S += r y0 / 2^53 = w y0 2^3, rounded in units of 2^8
+        S += (uint64_t)((int64_t)__float2int_rn((float)w * y0 * 0x1p-5f) * 256);
+    }
+    // second correction: |M - S^2| < 2^66, read as bits 36 .. 67
+    emu_sq_wide(S, hi, lo);
+    {
+        const uint64_t rlo = Mlo - lo, rhi = Mhi - hi - (Mlo < lo ? 1ull : 0ull);
+        const int32_t w = (int32_t)__funnelshift_r((uint32_t)(rlo >> 32), (uint32_t)rhi, 4);
+        S += (uint64_t)(int64_t)__float2int_rn((float)w * y0 * 0x1p-17f);
+    }
+    // the exact remainder (|r| < 2^56: the low word suffices), floor, rounding
+    int64_t r = (int64_t)(Mlo - S * S);
+    if (r < 0) {
+        S -= 1ull;
+        r += (int64_t)(2ull * S + 1ull);
+    }
+    if (r > (int64_t)(2ull * S)) {
+        r -= (int64_t)(2ull * S + 1ull);
+        S += 1ull;
+    }
+    const uint64_t Sr = S + (r > (int64_t)S ? 1ull : 0ull);  // [2^52, 2^53]
+    const int32_t er = ((int32_t)e - 1023 - (int32_t)odd) / 2 + 1023;  // exponent field of the result
+    uint64_t res = ((uint64_t)(uint32_t)(er - 1) << 52) + Sr;
+    const bool ok = e - 1u < 0x7feu;  // positive and normal
+    if (__any_sync(__activemask(), !ok)) {
+        if (!ok) res = emu_bits(emu_native_sqrt(x));
+    }
+    return emu_double(res);
+}
+
+// A divisor b prepared for several quotients: its significand mb and
+// inv ~ 2^115 / mb to within a few units (FP32 seed, two Newton corrections
+// inv += inv (2^115 - mb inv) / 2^115 on 32-bit windows of the exact
+// residual; the relative error falls from ~2^-21 to ~2^-42 to ~2^-61).
+struct EmuDivisor {
+    uint64_t mb, inv;
+    uint32_t bh;  // high word of b: sign and exponent
+};
+
+__device__ __forceinline__ EmuDivisor emu_divisor(double b) {
+    const uint64_t bb = emu_bits(b);
+    EmuDivisor D;
+    D.bh = (uint32_t)(bb >> 32);
+    D.mb = (bb & kEmuFrac) | kEmuHidden;
+    const float rf = __frcp_rn(__uint2float_rn((uint32_t)(D.mb >> 29)));  // ~ 2^29 / mb
+    uint64_t inv = (uint64_t)__float2uint_rn(rf * 0x1p46f) << 40;  // ~ 2^115 / mb
+    uint64_t hi = __umul64hi(D.mb, inv), lo = D.mb * inv;
+    {
+        // E = 2^115 - mb inv, |E| < 2^95: bits 64 .. 95; inv += inv E / 2^115
+        // = w rf 2^35, rounded in units of 2^16
+        const int32_t w = (int32_t)((1ull << 51) - hi - (lo != 0ull ? 1ull : 0ull));
+        inv += (uint64_t)((int64_t)__float2int_rn((float)w * rf * 0x1p19f) * 65536);
+    }
+    hi = __umul64hi(D.mb, inv);
+    lo = D.mb * inv;
+    {
+        // |E| < 2^75: bits 44 .. 75; inv += w rf 2^15
+        const uint64_t elo = 0ull - lo, ehi = (1ull << 51) - hi - (lo != 0ull ? 1ull : 0ull);
+        const int32_t w = (int32_t)__funnelshift_r((uint32_t)(elo >> 32), (uint32_t)ehi, 12);
+        inv += (uint64_t)(int64_t)__float2int_rn((float)w * rf * 0x1p15f);
+    }
+    D.inv = inv;
+    return D;
+}
+
+// RN(x / y) with D = emu_divisor(y). The significand quotient
+// Q = floor(ma 2^(52+s) / mb) (s = 1 when ma < mb, so Q is in [2^52, 2^53))
+// comes from ma inv to within one unit; the exact remainder
+// R = ma 2^(52+s) - Q mb makes Q the floor (0 <= R < mb) and rounds: up iff
+// 2R > mb (a quotient of two 53-bit significands is never a midpoint).
+// Long division by a scaled reciprocal with remainder correction, e.g.
+// R. Brent and P. Zimmermann, "Modern Computer Arithmetic", 2010, 1.4.1.
+__device__ __forceinline__ double emu_div(double x, const EmuDivisor &D, double y) {
+    const uint64_t a = emu_bits(x);
+    const uint32_t ah = (uint32_t)(a >> 32);
+    const uint32_t ea = (ah >> 20) & 0x7ffu, eb = (D.bh >> 20) & 0x7ffu;
+    const uint64_t ma = (a & kEmuFrac) | kEmuHidden;
+    const uint32_t s = ma < D.mb ? 1u : 0u;
+    uint64_t Q = __umul64hi(ma << 11, D.inv) >> (10u - s);
+    int64_t R = (int64_t)((ma << (52u + s)) - Q * D.mb);
+    if (R < 0) {
+        Q -= 1ull;
+        R += (int64_t)D.mb;
+    }
+    if (R >= (int64_t)D.mb) {
+        Q += 1ull;
+        R -= (int64_t)D.mb;
+    }
+    const uint64_t up = (uint64_t)(2 * R) > D.mb ? 1ull : 0ull;
+    const int e = (int)ea - (int)eb + 1023 - (int)s;  // biased exponent before rounding
+    const uint64_t sign = (uint64_t)((ah ^ D.bh) & 0x80000000u) << 32;
+    uint64_t r = sign | ((((uint64_t)(e - 1)) << 52) + Q + up);
+    const bool bn = eb - 1u < 0x7feu;
+    bool ok = bn && ea - 1u < 0x7feu && (uint32_t)(e - 1) < 2046u;
+    if (bn && (a & ~kEmuSign) == 0ull) {  // +-0 / b
+        r = sign;
+        ok = true;
+    }
+    if (__any_sync(__activemask(), !ok)) {
+        if (!ok) r = emu_bits(emu_native_div(x, y));
+    }
+    return emu_double(r);
+}
+
 __device__ __forceinline__ double emu_add(double x, double y) { return emu_addsub<false>(x, y); }
 __device__ __forceinline__ double emu_sub(double x, double y) { return emu_addsub<true>(x, y); }
+
+// Out-of-line copies, one body per translation unit, for kernels whose loops
+// would outgrow the instruction cache with every operation inlined (the FP64
+// force kernel: inlined, ncu counted 4.5 cycles of "no instruction" stall per
+// issued instruction; out of line, the kernel ran 1.3x faster). Kernels with
+// short loops (the density) keep the inlined forms.
+static __device__ __noinline__ double emu_mul_ol(double x, double y) { return emu_mul(x, y); }
+static __device__ __noinline__ double emu_sqrt_ol(double x) { return emu_sqrt(x); }
+static __device__ __noinline__ EmuDivisor emu_divisor_ol(double b) { return emu_divisor(b); }
+static __device__ __noinline__ double emu_div_ol(double x, const EmuDivisor &D, double y) { return emu_div(x, D, y); }
 
 }  // namespace sphgpu

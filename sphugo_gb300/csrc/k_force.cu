@@ -159,7 +159,7 @@ __device__ __forceinline__ void pair_geom(const SimDev &S, const PArrays &B, uin
         rabx = __dsub_rn(__dsub_rn(Q.x, ox), P.x);
         raby = __dsub_rn(__dsub_rn(Q.y, oy), P.y);
     }
-    dot = __dadd_rn(emu_mul(vabx, rabx), emu_mul(vaby, raby));
+    dot = __dadd_rn(emu_mul_ol(vabx, rabx), emu_mul_ol(vaby, raby));
 }
 
 template <int MODE>
@@ -283,10 +283,11 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                 const double rhoab = __dmul_rn(0.5, __dadd_rn(dp.y, dj.y));
                 const double hab = __dmul_rn(0.5, __dadd_rn(dp.z, dj.z));
                 const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
-                const double mu = __ddiv_rn(__dmul_rn(dot, hab), __dadd_rn(r2, Sp.etasq));
-                spi[e * 32 + p] = __ddiv_rn(__dadd_rn(__dmul_rn(__dmul_rn(-Sp.alpha, cab), mu),
-                                                      __dmul_rn(__dmul_rn(Sp.beta, mu), mu)),
-                                            rhoab);
+                const double den = __dadd_rn(r2, Sp.etasq);
+                const double mu = emu_div_ol(emu_mul_ol(dot, hab), emu_divisor_ol(den), den);
+                spi[e * 32 + p] = emu_div_ol(__dadd_rn(emu_mul_ol(emu_mul_ol(-Sp.alpha, cab), mu),
+                                                       emu_mul_ol(emu_mul_ol(Sp.beta, mu), mu)),
+                                             emu_divisor_ol(rhoab), rhoab);
             } else {
                 const double cab = 0.5 * (dp.x + dj.x), rhoab = 0.5 * (dp.y + dj.y), hab = 0.5 * (dp.z + dj.z);
                 const double mu = dot * hab / (rabx * rabx + raby * raby + Sp.etasq);
@@ -312,11 +313,11 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
                     const double piab = visc ? spi[e * 32 + lane] : 0.0;
                     const double cb = D.der[code >> kCodeShift].w;
                     const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
-                    // both quotients by NNDists[i] share RN(1/d) (div_rn_recip == __ddiv_rn)
-                    const double yd = __drcp_rn(d);
-                    ax = __dadd_rn(ax, div_rn_recip(emu_mul(emu_mul(rabx, sum3), drk), d, yd));
-                    ay = __dadd_rn(ay, div_rn_recip(emu_mul(emu_mul(raby, sum3), drk), d, yd));
-                    ed = __dadd_rn(ed, emu_mul(dot, drk));
+                    // both quotients by NNDists[i] share one prepared divisor
+                    const EmuDivisor dd = emu_divisor_ol(d);
+                    ax = __dadd_rn(ax, emu_div_ol(emu_mul_ol(emu_mul_ol(rabx, sum3), drk), dd, d));
+                    ay = __dadd_rn(ay, emu_div_ol(emu_mul_ol(emu_mul_ol(raby, sum3), drk), dd, d));
+                    ed = __dadd_rn(ed, emu_mul_ol(dot, drk));
                 });
                 const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
                 axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);

@@ -940,7 +940,7 @@ __global__ void __launch_bounds__(kTileWarps * 32, (MODE == MODE_MIXED || NR > 2
 // five resident blocks (48 registers): the FP64 forms' first loop waits on the
 // neighbour gathers, and more resident warps hide them (2.06 -> 2.02 ms at N = 1M)
 template <int MODE>
-__global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
+__global__ void __launch_bounds__(256, 4) k_density(KnnArgs a) {
     const int k = a.c.k;
     const PArrays &B = a.B;
     unsigned fl = 0;
@@ -962,15 +962,15 @@ __global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
             const int32_t *nb = a.D.nbr + q * k;
             const double dk2 = nbr_d2(S, B, P, (uint32_t)nb[k - 1]);
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
-            h = __dsqrt_rn(dk2);
-            const double yh = __drcp_rn(h);  // RN(1/h), shared by the k quotients d/h
+            h = emu_sqrt(dk2);
+            const EmuDivisor dh = emu_divisor(h);  // shared by the k quotients d/h
             // NNDists and q = NNDists/h; q grows with e (the list is sorted), so
             // the entries with q < 0.5 are a prefix of length s
             int s_lo = 0;
             for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {
-                const double d = e == k - 1 ? h : __dsqrt_rn(nbr_d2(S, B, P, code));
-                // == __ddiv_rn(d, h); in [0, 1] because d <= h
-                const double x = div_rn_recip(d, h, yh);
+                const double d = e == k - 1 ? h : emu_sqrt(nbr_d2(S, B, P, code));
+                // RN(d / h); in [0, 1] because d <= h
+                const double x = emu_div(d, dh, h);
                 s_lo += __double_as_longlong(x) < __double_as_longlong(0.5);  // x < 0.5 (x >= 0)
                 dist[e] = make_double2(d, x);
             });
@@ -999,17 +999,19 @@ __global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
                     dist[e].y = __dsub_rn(emu_mul(emu_mul(3.0, x), x), emu_mul(2.0, x));
                 }
             }
-            rho = __ddiv_rn(__dmul_rn(__dmul_rn(S.fpref, S.mass), acc), __dmul_rn(h, h));
+            const double hh = __dmul_rn(h, h);
+            rho = emu_div(__dmul_rn(__dmul_rn(S.fpref, S.mass), acc), emu_divisor(hh), hh);
             if (!(rho >= 0.0 && rho < 1.0e308)) fl |= FLAG_Q_RANGE;  // a NaN or infinite distance
-            cs = __dsqrt_rn(__dmul_rn(__dmul_rn(gamma, __dsub_rn(gamma, 1.0)), up));
-            cterm = __ddiv_rn(__dmul_rn(cs, cs), __dmul_rn(gamma, rho));
+            cs = emu_sqrt(__dmul_rn(__dmul_rn(gamma, __dsub_rn(gamma, 1.0)), up));
+            const double grho = __dmul_rn(gamma, rho);
+            cterm = emu_div(__dmul_rn(cs, cs), emu_divisor(grho), grho);
         } else if (MODE == MODE_FAST64) {
             double2 *dist = a.D.dist + q * k;
             const double2 P = B.pos[q];
             const int32_t *nb = a.D.nbr + q * k;
             const double dk2 = nbr_d2(S, B, P, (uint32_t)nb[k - 1]);
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
-            h = __dsqrt_rn(dk2);
+            h = emu_sqrt(dk2);
             const double inv_h = 1.0 / h;
             // q and 1/NNDists first; then the kernel sums and dF in branch-split
             // loops (q grows with e), leaving (dF, dF / NNDists) for the force
@@ -1051,7 +1053,7 @@ __global__ void __launch_bounds__(256, 5) k_density(KnnArgs a) {
             // FP64 only where it decides: the k-th neighbour's squared distance and h
             const double dk2 = nbr_d2(S, B, B.pos[q], (uint32_t)a.D.nbr[q * k + k - 1]);
             if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
-            h = __dsqrt_rn(dk2);
+            h = emu_sqrt(dk2);
             // everything after h in FP32 (prefactors from FP32 copies)
             const float hf = __double2float_rn(h);
             const float inv_hf = 1.f / hf;

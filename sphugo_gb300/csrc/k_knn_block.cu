@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                     if (fuse) {
                         const double dk2 = nbr_d2(S, B, B.pos[q], sm.code[kth & BS::SMASK]);
                         if (!(dk2 < 0.4)) fl |= FLAG_SENTINEL;
-                        hq = __dsqrt_rn(dk2);
+                        hq = emu_sqrt(dk2);
                         inv_hf = 1.f / __double2float_rn(hq);
                     }
                     KahanF acc;  // farthest first, the order of k_density's sum

@@ -405,6 +405,28 @@ __global__ void k_emu_selftest(int64_t n, uint64_t seed, unsigned long long *bad
         if (!emu_same(emu_mul(x, y), __dmul_rn(x, y))) nb++;
         if (!emu_same(emu_add(x, y), __dadd_rn(x, y))) nb++;
         if (!emu_same(emu_sub(x, y), __dsub_rn(x, y))) nb++;
+        // square roots: the operands above, and squares of random 53-bit and
+        // 26-bit significands moved by -2 .. +2 ulp (results next to rounding
+        // midpoints and exact)
+        double z = x;
+        if (cls == 1 || cls == 4) {
+            const double sq = emu_double(((uint64_t)(512u + (uint32_t)(r3 % 1024u)) << 52) | (r1 & kEmuFrac));
+            z = emu_double(emu_bits(__dmul_rn(sq, sq)) + (uint64_t)((int64_t)((r2 >> 3) % 5u) - 2));
+        } else if (cls == 2) {
+            const double sq = emu_double(((uint64_t)(512u + (uint32_t)(r3 % 1024u)) << 52) | (r1 & 0x000FFFFFFC000000ull));
+            z = __dmul_rn(sq, sq);  // exact: a perfect square
+        }
+        if (!emu_same(emu_sqrt(z), __dsqrt_rn(z))) nb++;
+        // quotients: the operand pairs above (class 2: short significands,
+        // exact quotients), and a = RN(b q) moved by -2 .. +2 ulp for random
+        // significands q (quotients next to rounding boundaries)
+        double num = x, den = y;
+        if (cls == 1 && ((r3 >> 24) & 1u)) {
+            const double q = emu_double((1023ull << 52) | (r1 & kEmuFrac));
+            num = emu_double(emu_bits(__dmul_rn(y, q)) + (uint64_t)((int64_t)((r2 >> 5) % 5u) - 2));
+        }
+        const EmuDivisor dv = emu_divisor(den);
+        if (!emu_same(emu_div(num, dv, den), __ddiv_rn(num, den))) nb++;
     }
     if (nb) atomicAdd(bad, nb);
 }
