@@ -25,10 +25,10 @@
 // subnormals, infinities, NaNs, overflow in a sum, underflow) and sums of
 // operands more than 63 binades apart take the hardware instruction, so
 // those rare cases need no integer code at all.
-// That instruction sits behind a branch that the warp takes only when one of
-// its active lanes needs it, in a function that is never inlined: a fallback
-// the compiler could compute speculatively (and select) would occupy the
-// FP64 unit on every call.
+// That instruction sits in a function that is never inlined, behind a
+// branch: a fallback the compiler could compute speculatively (and select)
+// would occupy the FP64 unit on every call (measured: the emulated product
+// then ran no faster than the hardware's).
 #pragma once
 #include <stdint.h>
 
@@ -102,9 +102,7 @@ __device__ __forceinline__ double emu_mul(double x, double y) {
     const uint32_t rhi = ((ah ^ bh) & 0x80000000u) | (((uint32_t)(e - 1) << 20) + mhi);
     uint64_t r = (((uint64_t)rhi << 32) | mlo) + up;
     const bool ok = ea - 1u < 0x7feu && eb - 1u < 0x7feu && (uint32_t)(e - 1) < 2046u;
-    if (__any_sync(__activemask(), !ok)) {
-        if (!ok) r = emu_bits(emu_native_mul(x, y));
-    }
+    if (!ok) r = emu_bits(emu_native_mul(x, y));
     return emu_double(r);
 }
 
@@ -149,9 +147,7 @@ __device__ __forceinline__ double emu_addsub(double x, double y) {
         r = big;
         ok = true;
     }
-    if (__any_sync(__activemask(), !ok)) {
-        if (!ok) r = emu_bits(SUB ? emu_native_sub(x, y) : emu_native_add(x, y));
-    }
+    if (!ok) r = emu_bits(SUB ? emu_native_sub(x, y) : emu_native_add(x, y));
     return emu_double(r);
 }
 
@@ -214,9 +210,7 @@ __device__ __forceinline__ double emu_sqrt(double x) {
     const int32_t er = ((int32_t)e - 1023 - (int32_t)odd) / 2 + 1023;  // exponent field of the result
     uint64_t res = ((uint64_t)(uint32_t)(er - 1) << 52) + Sr;
     const bool ok = e - 1u < 0x7feu;  // positive and normal
-    if (__any_sync(__activemask(), !ok)) {
-        if (!ok) res = emu_bits(emu_native_sqrt(x));
-    }
+    if (!ok) res = emu_bits(emu_native_sqrt(x));
     return emu_double(res);
 }
 
@@ -288,9 +282,7 @@ __device__ __forceinline__ double emu_div(double x, const EmuDivisor &D, double 
         r = sign;
         ok = true;
     }
-    if (__any_sync(__activemask(), !ok)) {
-        if (!ok) r = emu_bits(emu_native_div(x, y));
-    }
+    if (!ok) r = emu_bits(emu_native_div(x, y));
     return emu_double(r);
 }
 
