@@ -228,8 +228,9 @@ int sph_probe_peaks(double *fp64_tflops, double *fp32_tflops, double *div_cost, 
  * the process exits. x, y (n each) and the outputs are device-accessible
  * pointers; any output may be NULL: nbr_ids / nbr_dist (n*k, slot 0 =
  * farthest, as sph_get_neighbours), rho and hsml (n). stream is a
- * cudaStream_t (NULL = the default stream); the call returns after its work
- * on that stream is done. n <= SPH_NOALLOC_MAX_N and k <= SPH_NOALLOC_MAX_K,
+ * cudaStream_t (NULL = the default stream); the call is synchronous: it
+ * returns after its work on that stream is done (it reads its status back
+ * and waits), so it cannot be captured in a CUDA graph. n <= SPH_NOALLOC_MAX_N and k <= SPH_NOALLOC_MAX_K,
  * else SPH_ERR_ARG. The first call on a device looks up the scratch's device
  * address and sets kernel attributes, so make it before any stream capture.
  * All calls share the scratch: calls that overlap on the GPU (other threads
