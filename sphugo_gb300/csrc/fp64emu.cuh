@@ -297,6 +297,7 @@ __device__ __forceinline__ double emu_sub(double x, double y) { return emu_addsu
 static __device__ __noinline__ double emu_mul_ol(double x, double y) { return emu_mul(x, y); }
 static __device__ __noinline__ double emu_sqrt_ol(double x) { return emu_sqrt(x); }
 static __device__ __noinline__ EmuDivisor emu_divisor_ol(double b) { return emu_divisor(b); }
-static __device__ __noinline__ double emu_div_ol(double x, const EmuDivisor &D, double y) { return emu_div(x, D, y); }
+// (the divisor by value: by reference it went through the stack, 5 % of the force's time)
+static __device__ __noinline__ double emu_div_ol(double x, EmuDivisor D, double y) { return emu_div(x, D, y); }
 
 }  // namespace sphgpu
