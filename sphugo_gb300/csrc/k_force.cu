@@ -130,10 +130,11 @@ __global__ void __launch_bounds__(256, 4) k_force(ForceArgs a) {
 // and its order are unchanged, so the results stay bit-exact.
 constexpr int kForceWarps = 4;
 
-// per-warp shared memory: Pi doubles, masks, counts; rounded up to 16 bytes
-// so that every warp's Pi array starts 8-byte (in fact 16-byte) aligned
+// per-warp shared memory: Pi doubles of one chunk (at most 32 entries per
+// particle), masks, counts; rounded up to 16 bytes so that every warp's Pi
+// array starts 8-byte (in fact 16-byte) aligned
 __host__ __device__ constexpr size_t force_exact_warp_bytes(int k) {
-    return ((size_t)k * 256 + 4 * 32 * 4 + 33 * 4 + 15) & ~(size_t)15;
+    return ((size_t)(k < 32 ? k : 32) * 256 + 4 * 32 * 4 + 33 * 4 + 15) & ~(size_t)15;
 }
 constexpr bool force_exact_layout_aligned() {
     for (int k = 1; k <= 128; k++)
@@ -169,10 +170,10 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
     const int k = a.c.k;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nw = (k + 31) >> 5;  // mask words per particle (k <= 128)
-    // per warp: Pi[k][32] doubles, approach masks [4][32], inclusive pair counts [33]
+    // per warp: Pi[min(k, 32)][32] doubles, approach masks [4][32], inclusive pair counts [33]
     unsigned char *wb = smem_raw + (size_t)w * force_exact_warp_bytes(k);
     double *spi = (double *)wb;
-    uint32_t *smask = (uint32_t *)(wb + (size_t)k * 256);
+    uint32_t *smask = (uint32_t *)(wb + (size_t)(k < 32 ? k : 32) * 256);
     int32_t *sinc = (int32_t *)(smask + 4 * 32);
     const PArrays &B = a.B;
     const Derived &D = a.D;
@@ -189,7 +190,6 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
         // ---- 1. approaching pairs: the sign of v_AB . r_AB from the float-pair
         // records, with an error bound; the reference's FP64 dot product only
         // where the bound cannot decide (e.g. equal velocities)
-        int cnt = 0;
         if (valid) {
             P = B.pos[q];
             vpi = B.vp[q];
@@ -237,109 +237,114 @@ __global__ void __launch_bounds__(kForceWarps * 32) k_force_fp64(ForceArgs a) {
             for (int wd = 0; wd < 4; wd++) {
                 if (wd < nw) {
                     smask[wd * 32 + lane] = mw[wd];
-                    cnt += __popc(mw[wd]);
                 }
             }
         } else {
             for (int wd = 0; wd < nw; wd++) smask[wd * 32 + lane] = 0u;
         }
-        int inc = cnt;
+        // ---- 2 and 3 one chunk of 32 neighbour entries at a time (the chunk
+        // of mask word c: entries 32 c .. 32 c + 31), farthest chunk first, so
+        // the Pi table holds 32 entries per particle whatever k is; the sums run
+        // through the chunks in the reference's order (sim/sph.go:343,
+        // farthest first)
+        const double ca = di.w;
+        const double2 *dist = D.dist + q * k;
+        double ax = 0.0, ay = 0.0, ed = 0.0;
+        for (int c = nw - 1; c >= 0; c--) {
+            const int e_lo = 32 * c, e_hi = min(k, e_lo + 32);
+            const uint32_t mine = smask[c * 32 + lane];
+            int inc = __popc(mine);
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        sinc[lane] = inc;
-        const int total = __shfl_sync(0xffffffffu, inc, 31);
-        __syncwarp();
-        // ---- 2. Pi of every flagged pair of the warp's particles
-        for (int i = lane; i < total; i += 32) {
-            int p = 0;  // owner: the first lane whose inclusive count exceeds i
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            sinc[lane] = inc;
+            const int total = __shfl_sync(0xffffffffu, inc, 31);
+            __syncwarp();
+            // ---- 2. Pi of every flagged pair of the chunk
+            for (int i = lane; i < total; i += 32) {
+                int p = 0;  // owner: the first lane whose inclusive count exceeds i
 #pragma unroll
-            for (int b = 16; b > 0; b >>= 1)
-                if (sinc[p + b - 1] <= i) p += b;
-            int r = i - (p ? sinc[p - 1] : 0);  // r-th flagged pair of particle p
-            int e = 0;
-            for (int wd = 0; wd < nw; wd++) {
-                uint32_t m = smask[wd * 32 + p];
-                const int c = __popc(m);
-                if (r < c) {
-                    for (int t = 0; t < r; t++) m &= m - 1;
-                    e = wd * 32 + __ffs(m) - 1;
-                    break;
+                for (int b = 16; b > 0; b >>= 1)
+                    if (sinc[p + b - 1] <= i) p += b;
+                const int r = i - (p ? sinc[p - 1] : 0);  // r-th flagged pair of particle p in the chunk
+                uint32_t m = smask[c * 32 + p];
+                for (int t = 0; t < r; t++) m &= m - 1;
+                const int eo = __ffs(m) - 1;  // entry e_lo + eo
+                const int64_t qp = q0 + p;
+                const SimDev &Sp = a.c.sims[sim_of(a.c, qp)];
+                const double2 Pp = B.pos[qp], vpp = B.vp[qp];
+                const double4 dp = D.der[qp];
+                const uint32_t code = (uint32_t)D.nbr[qp * k + e_lo + eo];
+                double rabx, raby, dot;
+                pair_geom(Sp, B, code, Pp, vpp, rabx, raby, dot);
+                const double4 dj = D.der[code >> kCodeShift];
+                if (MODE == MODE_EXACT64) {
+                    const double cab = __dmul_rn(0.5, __dadd_rn(dp.x, dj.x));
+                    const double rhoab = __dmul_rn(0.5, __dadd_rn(dp.y, dj.y));
+                    const double hab = __dmul_rn(0.5, __dadd_rn(dp.z, dj.z));
+                    const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
+                    const double den = __dadd_rn(r2, Sp.etasq);
+                    const double mu = emu_div_ol(emu_mul_ol(dot, hab), emu_divisor_ol(den), den);
+                    spi[eo * 32 + p] = emu_div_ol(__dadd_rn(emu_mul_ol(emu_mul_ol(-Sp.alpha, cab), mu),
+                                                            emu_mul_ol(emu_mul_ol(Sp.beta, mu), mu)),
+                                                  emu_divisor_ol(rhoab), rhoab);
+                } else {
+                    const double cab = 0.5 * (dp.x + dj.x), rhoab = 0.5 * (dp.y + dj.y), hab = 0.5 * (dp.z + dj.z);
+                    const double mu = dot * hab / (rabx * rabx + raby * raby + Sp.etasq);
+                    spi[eo * 32 + p] = mu * (Sp.beta * mu - Sp.alpha * cab) / rhoab;
                 }
-                r -= c;
             }
-            const int64_t qp = q0 + p;
-            const SimDev &Sp = a.c.sims[sim_of(a.c, qp)];
-            const double2 Pp = B.pos[qp], vpp = B.vp[qp];
-            const double4 dp = D.der[qp];
-            const uint32_t code = (uint32_t)D.nbr[qp * k + e];
-            double rabx, raby, dot;
-            pair_geom(Sp, B, code, Pp, vpp, rabx, raby, dot);
-            const double4 dj = D.der[code >> kCodeShift];
-            if (MODE == MODE_EXACT64) {
-                const double cab = __dmul_rn(0.5, __dadd_rn(dp.x, dj.x));
-                const double rhoab = __dmul_rn(0.5, __dadd_rn(dp.y, dj.y));
-                const double hab = __dmul_rn(0.5, __dadd_rn(dp.z, dj.z));
-                const double r2 = __dadd_rn(__dmul_rn(rabx, rabx), __dmul_rn(raby, raby));
-                const double den = __dadd_rn(r2, Sp.etasq);
-                const double mu = emu_div_ol(emu_mul_ol(dot, hab), emu_divisor_ol(den), den);
-                spi[e * 32 + p] = emu_div_ol(__dadd_rn(emu_mul_ol(emu_mul_ol(-Sp.alpha, cab), mu),
-                                                       emu_mul_ol(emu_mul_ol(Sp.beta, mu), mu)),
-                                             emu_divisor_ol(rhoab), rhoab);
-            } else {
-                const double cab = 0.5 * (dp.x + dj.x), rhoab = 0.5 * (dp.y + dj.y), hab = 0.5 * (dp.z + dj.z);
-                const double mu = dot * hab / (rabx * rabx + raby * raby + Sp.etasq);
-                spi[e * 32 + p] = mu * (Sp.beta * mu - Sp.alpha * cab) / rhoab;
+            __syncwarp();
+            // ---- 3. the chunk's terms of the reference's ordered sums
+            if (valid) {
+                if (MODE == MODE_EXACT64) {
+                    for_each_nbr_desc_range(nb, e_lo, e_hi, k, [&](int e, uint32_t code) {
+                        const double d = dist[e].x;
+                        const double drk = dist[e].y;  // dF(NNDists[i]/maxR), evaluated by the density pass
+                        double rabx, raby, dot;
+                        pair_geom(S, B, code, P, vpi, rabx, raby, dot);
+                        const bool visc = (mine >> (e - e_lo)) & 1u;
+                        const double piab = visc ? spi[(e - e_lo) * 32 + lane] : 0.0;
+                        const double cb = D.der[code >> kCodeShift].w;
+                        const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
+                        // both quotients by NNDists[i] share one prepared divisor
+                        const EmuDivisor dd = emu_divisor_ol(d);
+                        ax = __dadd_rn(ax, emu_div_ol(emu_mul_ol(emu_mul_ol(rabx, sum3), drk), dd, d));
+                        ay = __dadd_rn(ay, emu_div_ol(emu_mul_ol(emu_mul_ol(raby, sum3), drk), dd, d));
+                        ed = __dadd_rn(ed, emu_mul_ol(dot, drk));
+                    });
+                } else {
+                    // the fast form keeps (dF, dF / NNDists) per neighbour
+                    for_each_nbr_desc_range(nb, e_lo, e_hi, k, [&](int e, uint32_t code) {
+                        const double2 dd = dist[e];
+                        const uint32_t j = code >> kCodeShift;
+                        const double2 vpj = B.vp[j], Q = B.pos[j];
+                        double ox = 0.0, oy = 0.0;
+                        if ((code & 15u) != 4u) img_shift(S, code & 15u, ox, oy);
+                        const double rabx = (Q.x - ox) - P.x, raby = (Q.y - oy) - P.y;
+                        const double dot = (vpj.x - vpi.x) * rabx + (vpj.y - vpi.y) * raby;
+                        const bool visc = (mine >> (e - e_lo)) & 1u;
+                        const double piab = visc ? spi[(e - e_lo) * 32 + lane] : 0.0;
+                        const double w = (piab + ca + D.der[j].w) * dd.y;
+                        ax += rabx * w;
+                        ay += raby * w;
+                        ed += dot * dd.x;
+                    });
+                }
             }
+            __syncwarp();
         }
-        __syncwarp();
-        // ---- 3. the reference's ordered sums
         if (valid) {
-            const double ci = di.x, rhoi = di.y, hi = di.z, ca = di.w;
-            (void)ci;
-            (void)rhoi;
-            const double2 *dist = D.dist + q * k;
-            double ax = 0.0, ay = 0.0, ed = 0.0;
+            const double hi = di.z;
             double axo, ayo, edot;
             if (MODE == MODE_EXACT64) {
-                for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {  // sim/sph.go:343, farthest first
-                    const double d = dist[e].x;
-                    const double drk = dist[e].y;  // dF(NNDists[i]/maxR), evaluated by the density pass
-                    double rabx, raby, dot;
-                    pair_geom(S, B, code, P, vpi, rabx, raby, dot);
-                    const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;
-                    const double piab = visc ? spi[e * 32 + lane] : 0.0;
-                    const double cb = D.der[code >> kCodeShift].w;
-                    const double sum3 = __dadd_rn(__dadd_rn(piab, ca), cb);
-                    // both quotients by NNDists[i] share one prepared divisor
-                    const EmuDivisor dd = emu_divisor_ol(d);
-                    ax = __dadd_rn(ax, emu_div_ol(emu_mul_ol(emu_mul_ol(rabx, sum3), drk), dd, d));
-                    ay = __dadd_rn(ay, emu_div_ol(emu_mul_ol(emu_mul_ol(raby, sum3), drk), dd, d));
-                    ed = __dadd_rn(ed, emu_mul_ol(dot, drk));
-                });
                 const double f = __ddiv_rn(__dmul_rn(S.mass, S.dfpref), __dmul_rn(__dmul_rn(hi, hi), hi));
                 axo = __dadd_rn(__dmul_rn(ax, f), S.accel[0]);
                 ayo = __dadd_rn(__dmul_rn(ay, f), S.accel[1]);
                 edot = __dmul_rn(__dmul_rn(ca, ed), S.mass);
             } else {
-                // the fast form keeps (dF, dF / NNDists) per neighbour
-                for_each_nbr_desc(nb, k, [&](int e, uint32_t code) {
-                    const double2 dd = dist[e];
-                    const uint32_t j = code >> kCodeShift;
-                    const double2 vpj = B.vp[j], Q = B.pos[j];
-                    double ox = 0.0, oy = 0.0;
-                    if ((code & 15u) != 4u) img_shift(S, code & 15u, ox, oy);
-                    const double rabx = (Q.x - ox) - P.x, raby = (Q.y - oy) - P.y;
-                    const double dot = (vpj.x - vpi.x) * rabx + (vpj.y - vpi.y) * raby;
-                    const bool visc = (smask[(e >> 5) * 32 + lane] >> (e & 31)) & 1u;
-                    const double piab = visc ? spi[e * 32 + lane] : 0.0;
-                    const double w = (piab + ca + D.der[j].w) * dd.y;
-                    ax += rabx * w;
-                    ay += raby * w;
-                    ed += dot * dd.x;
-                });
                 const double inv_h = 1.0 / hi;
                 const double f = S.mass * S.dfpref * (inv_h * inv_h * inv_h);
                 axo = ax * f + S.accel[0];

@@ -122,6 +122,24 @@ __device__ __forceinline__ void for_each_nbr_desc(const int32_t *nb, int k, F f)
     }
 }
 
+// entries hi-1 down to lo of a list of k entries (16-byte loads when k, and
+// with it every bound used here, is a multiple of four)
+template <typename F>
+__device__ __forceinline__ void for_each_nbr_desc_range(const int32_t *nb, int lo, int hi, int k, F f) {
+    if ((k & 3) == 0) {
+        const int4 *nb4 = reinterpret_cast<const int4 *>(nb);
+        for (int b = (hi >> 2) - 1; b >= (lo >> 2); b--) {
+            const int4 c = nb4[b];
+            f(4 * b + 3, (uint32_t)c.w);
+            f(4 * b + 2, (uint32_t)c.z);
+            f(4 * b + 1, (uint32_t)c.y);
+            f(4 * b, (uint32_t)c.x);
+        }
+    } else {
+        for (int e = hi - 1; e >= lo; e--) f(e, (uint32_t)nb[e]);
+    }
+}
+
 // r_AB = (q - offset) - p from the float-pair records of the neighbour (r)
 // and the particle (pr), image code img (4 = no shift): the high parts'
 // difference is exact by Sterbenz for neighbours within a period, so the
