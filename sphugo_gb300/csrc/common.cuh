@@ -14,6 +14,7 @@
 #include <string>
 
 #include "../../include/sphgpu.h"
+#include "fp64emu.cuh"
 
 namespace sphgpu {
 
@@ -171,8 +172,7 @@ __host__ __device__ inline double dkey_inv(unsigned long long k) {
 
 // double -> (hi, lo) float pair
 __device__ __forceinline__ void split_df(double v, float &hi, float &lo) {
-    hi = __double2float_rn(v);
-    lo = __double2float_rn(__dsub_rn(v, (double)hi));
+    emu_split_df(v, hi, lo);  // hi = RN_float(v), lo = RN_float(v - hi), on the integer pipes
 }
 
 // The drift of sim/sph.go:108-117 (no contraction: two roundings each).
@@ -181,11 +181,11 @@ __device__ __forceinline__ void predict(const SimDev &S, int mode, double2 pos, 
                                         double up_old, double2 &p, double2 &vp, double &up) {
     if (mode == PRED_DRIFT) {
         double dth = S.dth;
-        p.x = __dadd_rn(pos.x, __dmul_rn(vel.x, dth));
-        p.y = __dadd_rn(pos.y, __dmul_rn(vel.y, dth));
-        vp.x = __dadd_rn(vel.x, __dmul_rn(acc.x, dth));
-        vp.y = __dadd_rn(vel.y, __dmul_rn(acc.y, dth));
-        up = __dadd_rn(u, __dmul_rn(udot, dth));
+        p.x = __dadd_rn(pos.x, emu_mul(vel.x, dth));
+        p.y = __dadd_rn(pos.y, emu_mul(vel.y, dth));
+        vp.x = __dadd_rn(vel.x, emu_mul(acc.x, dth));
+        vp.y = __dadd_rn(vel.y, emu_mul(acc.y, dth));
+        up = __dadd_rn(u, emu_mul(udot, dth));
     } else if (mode == PRED_INIT) {
         p = pos; vp = vel; up = u;
     } else {

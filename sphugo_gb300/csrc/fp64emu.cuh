@@ -1,6 +1,7 @@
 // fp64emu.cuh -- binary64 multiplication, addition, subtraction, division
 // and square root, rounded to nearest with ties to even (IEEE 754-2019,
-// 4.3.1), computed with integer instructions (and FP32 seeds).
+// 4.3.1), and the split of a binary64 into a float pair, computed with
+// integer instructions (and FP32 seeds and conversions).
 //
 // GB300 issues two FP64 lanes per SM per clock: one warp-wide FP64
 // instruction holds a sub-partition's FP64 unit for about 64 cycles, while
@@ -104,6 +105,34 @@ __device__ __forceinline__ double emu_mul(double x, double y) {
     const bool ok = ea - 1u < 0x7feu && eb - 1u < 0x7feu && (uint32_t)(e - 1) < 2046u;
     if (!ok) r = emu_bits(emu_native_mul(x, y));
     return emu_double(r);
+}
+
+// The float pair of v: hi = RN_float(v) and lo = RN_float(v - hi) (v - hi is
+// exact in binary64). hi rounds the 53-bit significand to 24 bits; the
+// remainder t = m - hi's significand 2^29 is an integer below 2^29 in
+// magnitude, converted by the FP32 integer conversion (one rounding) and
+// scaled by 2^(e - 1075) through its exponent field. Operands whose pair
+// parts would leave the normal float range take the hardware conversions.
+__device__ __forceinline__ void emu_split_df(double v, float &hi, float &lo) {
+    const uint64_t a = emu_bits(v);
+    const uint32_t ah = (uint32_t)(a >> 32);
+    const uint32_t e = (ah >> 20) & 0x7ffu;
+    const uint64_t m = (a & kEmuFrac) | kEmuHidden;
+    const uint32_t q = (uint32_t)(m >> 29), rem = (uint32_t)m & 0x1fffffffu;
+    const uint32_t qh = q + ((rem > 0x10000000u || (rem == 0x10000000u && (q & 1u))) ? 1u : 0u);  // <= 2^24
+    // exponent field e - 896 with the hidden bit of qh adding one (a carry to
+    // 2^24 adds one more)
+    const uint32_t hb = (ah & 0x80000000u) | (((e - 897u) << 23) + qh);
+    const int32_t t = (int32_t)((uint32_t)m & 0x1fffffffu) - (int32_t)((qh - q) << 29);  // m - qh 2^29
+    const float tf = __int2float_rn((ah & 0x80000000u) ? -t : t);
+    const uint32_t lb = __float_as_uint(tf) + ((e - 1075u) << 23);  // tf 2^(e - 1075)
+    bool ok = e - 950u < 200u;  // hi and lo (if not zero) normal floats
+    hi = __uint_as_float(hb);
+    lo = t == 0 ? 0.f : __uint_as_float(lb);
+    if (!ok) {
+        hi = __double2float_rn(v);
+        lo = __double2float_rn(emu_native_sub(v, (double)hi));
+    }
 }
 
 // RN(x + y) (SUB = false) or RN(x - y) (SUB = true). The smaller operand's

@@ -427,6 +427,17 @@ __global__ void k_emu_selftest(int64_t n, uint64_t seed, unsigned long long *bad
         }
         const EmuDivisor dv = emu_divisor(den);
         if (!emu_same(emu_div(num, dv, den), __ddiv_rn(num, den))) nb++;
+        // float pairs of the operands and of the products
+        float h1, l1;
+        emu_split_df(x, h1, l1);
+        const float h0 = __double2float_rn(x), l0 = __double2float_rn(__dsub_rn(x, (double)h0));
+        if (__float_as_uint(h1) != __float_as_uint(h0) && !(h1 != h1 && h0 != h0)) nb++;
+        if (__float_as_uint(l1) != __float_as_uint(l0) && !(l1 != l1 && l0 != l0)) nb++;
+        const double xy = __dmul_rn(x, y);
+        emu_split_df(xy, h1, l1);
+        const float h2 = __double2float_rn(xy), l2 = __double2float_rn(__dsub_rn(xy, (double)h2));
+        if (__float_as_uint(h1) != __float_as_uint(h2) && !(h1 != h1 && h2 != h2)) nb++;
+        if (__float_as_uint(l1) != __float_as_uint(l2) && !(l1 != l1 && l2 != l2)) nb++;
     }
     if (nb) atomicAdd(bad, nb);
 }

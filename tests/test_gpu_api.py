@@ -117,11 +117,11 @@ def test_division_sequences_are_correctly_rounded(gpu):
 
 def test_integer_pipe_fp64_operations_match_the_hardware(gpu):
     """The FP64 kernels compute some multiplications, additions,
-    subtractions, divisions and square roots with integer instructions; each
-    must return the hardware instruction's bits. 5 x 2^31 results over random
-    bit patterns, nearby and extreme exponents, exact ties, near
-    cancellation, perfect squares and their neighbours, quotients next to
-    rounding boundaries, and special values."""
+    subtractions, divisions, square roots and float-pair splits with integer
+    instructions; each must return the hardware instruction's bits. 9 x 2^31
+    results over random bit patterns, nearby and extreme exponents, exact
+    ties, near cancellation, perfect squares and their neighbours, quotients
+    next to rounding boundaries, and special values."""
     bad = C.c_int64(-1)
     L.check(gpu.sph_selftest_fp64emu(1 << 31, 2024, C.byref(bad)))
     assert bad.value == 0
