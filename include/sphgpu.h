@@ -249,10 +249,10 @@ int sph_density_noalloc(const sph_params *p, const double *x, const double *y, i
 int sph_selftest_division(int64_t n, uint64_t seed, int64_t *mismatches);
 
 /* Self-check (no reference counterpart): runs the library's binary64
- * multiplication, addition, subtraction, division and square root, and its
- * binary64 -> (float, float) splits, computed with integer instructions
- * (which the FP64 kernels use beside the hardware FP64 unit) against the
- * hardware instructions on 9 n results from n seeded
+ * multiplication, addition, subtraction, division and square root, its
+ * 1 - x for x in [1/2, 1] and its binary64 -> (float, float) splits, computed
+ * with integer instructions (which the FP64 kernels use beside the hardware
+ * FP64 unit) against the hardware instructions on 12 n results from n seeded
  * operand pairs (random bits, nearby and extreme exponents, exact ties, near
  * cancellation, perfect squares and their neighbours, quotients next to
  * rounding boundaries, zeros, subnormals,

@@ -107,6 +107,19 @@ __device__ __forceinline__ double emu_mul(double x, double y) {
     return emu_double(r);
 }
 
+// RN(1 - x) for x in [1/2, 1], where the difference is exact (Sterbenz):
+// 1 - x = (2^53 - m) 2^-53 for the significand m of x in [1/2, 1), shifted to
+// put its leading bit at bit 52. Other x take the hardware subtraction.
+__device__ __forceinline__ double emu_one_minus(double x) {
+    const uint64_t a = emu_bits(x);
+    const uint64_t t = (1ull << 53) - ((a & kEmuFrac) | kEmuHidden);  // in (0, 2^52]
+    const int lz = __clzll((long long)t) - 11;  // 0 .. 52
+    uint64_t r = (((uint64_t)(1021 - lz)) << 52) + (t << lz);
+    if (a == 0x3FF0000000000000ull) r = 0ull;  // 1 - 1 = +0
+    else if ((a >> 52) != 1022ull) r = emu_bits(emu_native_sub(1.0, x));
+    return emu_double(r);
+}
+
 // The float pair of v: hi = RN_float(v) and lo = RN_float(v - hi) (v - hi is
 // exact in binary64). hi rounds the 53-bit significand to 24 bits; the
 // remainder t = m - hi's significand 2^29 is an integer below 2^29 in

@@ -987,7 +987,7 @@ __global__ void __launch_bounds__(256, 4) k_density(KnnArgs a) {
             } else {
                 for (int e = k - 1; e >= s_lo; e--) {  // q >= 0.5
                     const double x = dist[e].y;
-                    const double a1 = __dsub_rn(1.0, x);
+                    const double a1 = emu_one_minus(x);  // x in [1/2, 1]: exact
                     const double a2 = emu_mul(a1, a1);
                     acc = __dadd_rn(acc, div3_rn(emu_mul(a2, a1)));
                     dist[e].y = -a2;

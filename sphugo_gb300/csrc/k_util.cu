@@ -427,6 +427,11 @@ __global__ void k_emu_selftest(int64_t n, uint64_t seed, unsigned long long *bad
         }
         const EmuDivisor dv = emu_divisor(den);
         if (!emu_same(emu_div(num, dv, den), __ddiv_rn(num, den))) nb++;
+        // 1 - x, for x in [1/2, 1] from the operand's significand and for the operand itself
+        const double xh = emu_double((1022ull << 52) | (r1 & kEmuFrac));
+        if (!emu_same(emu_one_minus(xh), __dsub_rn(1.0, xh))) nb++;
+        if (!emu_same(emu_one_minus(x), __dsub_rn(1.0, x))) nb++;
+        if (!emu_same(emu_one_minus(1.0), __dsub_rn(1.0, 1.0))) nb++;
         // float pairs of the operands and of the products
         float h1, l1;
         emu_split_df(x, h1, l1);

@@ -118,7 +118,7 @@ def test_division_sequences_are_correctly_rounded(gpu):
 def test_integer_pipe_fp64_operations_match_the_hardware(gpu):
     """The FP64 kernels compute some multiplications, additions,
     subtractions, divisions, square roots and float-pair splits with integer
-    instructions; each must return the hardware instruction's bits. 9 x 2^31
+    instructions; each must return the hardware instruction's bits. 12 x 2^31
     results over random bit patterns, nearby and extreme exponents, exact
     ties, near cancellation, perfect squares and their neighbours, quotients
     next to rounding boundaries, and special values."""
