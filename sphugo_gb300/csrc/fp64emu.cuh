@@ -9,12 +9,14 @@
 // cycle. The FP64-bound kernels leave about 90 % of the issue slots idle, so
 // some of their operations are computed here, on the integer and FP32
 // pipes, in parallel with the hardware FP64 instructions. Every result is
-// the hardware instruction's, bit for bit (sph_selftest_fp64emu checks this
-// against __dmul_rn / __dadd_rn / __dsub_rn).
+// the hardware instruction's, bit for bit (sph_selftest_fp64emu checks each
+// against __dmul_rn, __dadd_rn, __dsub_rn, __ddiv_rn, __dsqrt_rn and the
+// double -> float conversion).
 //
-// Method (the textbook guard digits and sticky bit, e.g. D. Goldberg, "What
-// every computer scientist should know about floating-point arithmetic",
-// ACM Computing Surveys 23(1), 1991):
+// Method for products and sums (the textbook guard digits and sticky bit,
+// e.g. D. Goldberg, "What every computer scientist should know about
+// floating-point arithmetic", ACM Computing Surveys 23(1), 1991; quotients
+// and square roots are described at their functions):
 //   * product: the exact 106-bit product of the two 53-bit significands, its
 //     leading 53 bits rounded on the remaining bits (round bit, then "any
 //     bit below it" as the sticky);
@@ -35,42 +37,11 @@
 
 namespace sphgpu {
 
-#ifndef SPH_EMU_FALLBACK
-#define SPH_EMU_FALLBACK 1
-#endif
-#if SPH_EMU_FALLBACK == 1
 static __device__ __noinline__ double emu_native_mul(double x, double y) { return __dmul_rn(x, y); }
 static __device__ __noinline__ double emu_native_add(double x, double y) { return __dadd_rn(x, y); }
 static __device__ __noinline__ double emu_native_sub(double x, double y) { return __dsub_rn(x, y); }
 static __device__ __noinline__ double emu_native_sqrt(double x) { return __dsqrt_rn(x); }
 static __device__ __noinline__ double emu_native_div(double x, double y) { return __ddiv_rn(x, y); }
-#else
-__device__ __forceinline__ double emu_native_mul(double x, double y) {
-    double r;
-    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
-    return r;
-}
-__device__ __forceinline__ double emu_native_add(double x, double y) {
-    double r;
-    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
-    return r;
-}
-__device__ __forceinline__ double emu_native_sub(double x, double y) {
-    double r;
-    asm volatile("sub.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
-    return r;
-}
-__device__ __forceinline__ double emu_native_sqrt(double x) {
-    double r;
-    asm volatile("sqrt.rn.f64 %0, %1;" : "=d"(r) : "d"(x));
-    return r;
-}
-__device__ __forceinline__ double emu_native_div(double x, double y) {
-    double r;
-    asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(y));
-    return r;
-}
-#endif
 
 constexpr uint64_t kEmuSign = 0x8000000000000000ull;
 constexpr uint64_t kEmuFrac = 0x000FFFFFFFFFFFFFull;
