@@ -40,7 +40,9 @@ extern "C" {
 /* arithmetic form of density and force */
 #define SPH_PREC_FP64 0       /* plain FP64 drop-in: the reference's operation order, bit for bit */
 #define SPH_PREC_MIXED 1      /* FP32 relative-coordinate sums with compensation; FP64 kNN decisions, h and integrator */
-#define SPH_PREC_FP64_FAST 2  /* FP64 with contraction and per-particle reciprocals (within 1e-12 of SPH_PREC_FP64) */
+#define SPH_PREC_FP64_FAST 2  /* FP64 with contraction and per-particle reciprocals (within 1e-12 of SPH_PREC_FP64);
+                               * on GB300 slower than SPH_PREC_FP64, whose kernels move part of their FP64
+                               * work to the integer pipes */
 
 /* Simulation parameters: the fields of SphConfig that the step reads
  * (sim/config-parser.go:111-128) plus the constants the reference hard-codes
