@@ -428,14 +428,19 @@ def workload_case(kind, n, k, dt, seed, form, steps):
 
 
 def e2e_run(sim, steps):
-    """set_state from pinned host arrays + step + get_state, every step."""
+    """set_state from pinned host arrays + step + get_state, every step. The
+    arrays live in pinned memory from sph_host_alloc, as a caller keeping its
+    per-step state for the library would hold them."""
     import numpy as np
     from sphugo_gb300 import _lib as L
     lib = L.load()
     n = sim.n
-    bufs = [np.empty(n) for _ in range(8)]
-    for b in bufs:
-        L.check(lib.sph_host_register(b.ctypes.data, b.nbytes))
+    raw = []
+    for _ in range(8):
+        p = C.c_void_p()
+        L.check(lib.sph_host_alloc(8 * n, C.byref(p)))
+        raw.append(p)
+    bufs = [np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_double)), shape=(n,)) for p in raw]
     try:
         st = sim.state()
         for b, k in zip(bufs, ["x", "y", "vx", "vy", "u", "ax", "ay", "udot"]):
@@ -448,8 +453,9 @@ def e2e_run(sim, steps):
             L.check(lib.sph_get_state(sim._h, *ptrs))
         dt = time.perf_counter() - t0
     finally:
-        for b in bufs:
-            lib.sph_host_unregister(b.ctypes.data)
+        del bufs
+        for p in raw:
+            lib.sph_host_free(p)
     return dt, 8 * 8 * n, 8 * 8 * n
 
 

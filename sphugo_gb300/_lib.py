@@ -38,7 +38,7 @@ EXPORTS = [
     "sph_get_state", "sph_get_derived", "sph_error_norms", "sph_memory_bytes", "sph_get_neighbours", "sph_step",
     "sph_step_async", "sph_forces",
     "sph_synchronize", "sph_current_step", "sph_num_particles", "sph_host_register",
-    "sph_host_unregister", "sph_diagnostics", "sph_ic_uniform_blast", "sph_ic_clustered",
+    "sph_host_unregister", "sph_host_alloc", "sph_host_free", "sph_diagnostics", "sph_ic_uniform_blast", "sph_ic_clustered",
     "sph_ic_stress", "sph_ic_ensemble", "sph_config_default", "sph_config_load",
     "sph_config_start_count", "sph_config_spawn", "sph_point_source_spawn",
     "sph_step_timed", "sph_step_profiled", "sph_kernels_per_step", "sph_set_search", "sph_search_stats",
@@ -127,6 +127,8 @@ def load() -> C.CDLL:
     L.sph_num_particles.restype = C.c_int64
     L.sph_host_register.argtypes = [vp, C.c_int64]
     L.sph_host_unregister.argtypes = [vp]
+    L.sph_host_alloc.argtypes = [C.c_int64, C.POINTER(vp)]
+    L.sph_host_free.argtypes = [vp]
     L.sph_diagnostics.argtypes = [vp, C.c_int32, dp]
     L.sph_ic_uniform_blast.argtypes = [C.c_int64, C.c_uint64, C.c_double, C.c_double, C.c_double] + [dp] * 5
     L.sph_ic_clustered.argtypes = [C.c_int64, C.c_uint64, C.c_int32, C.c_double, C.c_double, C.c_double,

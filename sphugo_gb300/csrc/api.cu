@@ -918,6 +918,19 @@ int sph_host_unregister(void *ptr) {
     return SPH_OK;
 }
 
+int sph_host_alloc(int64_t bytes, void **ptr) {
+    if (!ptr || bytes <= 0) return fail(SPH_ERR_ARG, "bad pointer or size");
+    *ptr = nullptr;
+    CUDA_TRY(cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault));
+    return SPH_OK;
+}
+
+int sph_host_free(void *ptr) {
+    if (!ptr) return fail(SPH_ERR_ARG, "bad pointer");
+    CUDA_TRY(cudaFreeHost(ptr));
+    return SPH_OK;
+}
+
 int sph_step_timed(sph_handle *h, int32_t nsteps, double *ms) {
     if (!h || nsteps < 0 || !ms) return fail(SPH_ERR_ARG, "bad argument");
     Guard g(h);

@@ -77,6 +77,10 @@ def test_argument_checks_precede_device_use(sphlib):
     p = sphlib.sph_default_params()
     p.k = 0
     assert sphlib.sph_create(C.byref(p), 100, C.byref(h)) == L.SPH_ERR_ARG
+    ptr = C.c_void_p()
+    assert sphlib.sph_host_alloc(0, C.byref(ptr)) == L.SPH_ERR_ARG
+    assert sphlib.sph_host_alloc(64, None) == L.SPH_ERR_ARG
+    assert sphlib.sph_host_free(None) == L.SPH_ERR_ARG
 
 
 def test_uniform_blast_ic_is_deterministic_and_uniform(sphlib):

@@ -105,6 +105,40 @@ def test_checkpoint_rejects_other_parameters(gpu, tmp_path):
     assert e.value.code == L.SPH_ERR_ARG
 
 
+def test_state_round_trip_through_pinned_host_allocations(gpu):
+    """sph_set_state / sph_get_state from and to memory of sph_host_alloc:
+    the state read back equals the state written, bit for bit."""
+    import numpy as np
+    n = 20_000
+    x, y, vx, vy, u = ics.uniform_blast(n, 5)
+    s = S.Simulation(ics.periodic_config(n, 32, 1e-4, "Exact"), x, y, vx, vy, u)
+    s.Step(2)
+    st = s.state()
+    keys = ["x", "y", "vx", "vy", "u", "ax", "ay", "udot"]
+    raw = []
+    try:
+        for _ in keys:
+            p = C.c_void_p()
+            L.check(gpu.sph_host_alloc(8 * n, C.byref(p)))
+            raw.append(p)
+        bufs = [np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_double)), shape=(n,)) for p in raw]
+        for b, k in zip(bufs, keys):
+            b[:] = st[k] * 1.0
+        bufs[2][:] += 0.25  # a changed velocity must arrive
+        L.check(gpu.sph_set_state(s._h, *[L.dptr(b) for b in bufs]))
+        for b in bufs:
+            b[:] = 0.0
+        L.check(gpu.sph_get_state(s._h, *[L.dptr(b) for b in bufs]))
+        for b, k in zip(bufs, keys):
+            want = st[k] + (0.25 if k == "vx" else 0.0)
+            assert np.array_equal(b, want), k
+        del bufs
+    finally:
+        for p in raw:
+            gpu.sph_host_free(p)
+        s.close()
+
+
 def test_division_sequences_are_correctly_rounded(gpu):
     """The FP64 form replaces some IEEE divisions by FMA sequences that must
     return the same bits (division by 3; a shared reciprocal with a Markstein
