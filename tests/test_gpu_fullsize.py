@@ -4,9 +4,10 @@
     both arithmetic forms against the oracle's exact evaluation of the same
     state: neighbour sets bit-exact in both forms, the FP64 form bit-exact in
     every array, the mixed form within its stated tolerances;
-  * the clustered workload (N = 4,194,304, k = 32) at the end of the mixed
-    form's full 50-step run: both forms evaluate that final state; sets
-    bit-exact, mixed errors within the stated tolerances;
+  * the clustered workload (N = 4,194,304, k = 32): one force evaluation of
+    the FP64 form against the oracle, bit for bit; and at the
+    end of the mixed form's full 50-step run both forms evaluate its final
+    state: sets bit-exact, mixed errors within the stated tolerances;
   * the 256-simulation ensemble in the mixed form, simulation by simulation
     against the oracle; and in the FP64 form over its full 100 steps.
 
@@ -69,6 +70,33 @@ def test_stress_full_size_both_forms_against_oracle(gpu, oracle):
             assert r.max() <= RHO_TOL, r.max()
             assert a.max() <= ACC_TOL, a.max()
             assert ud.max() <= UDOT_TOL, ud.max()
+
+
+def test_clustered_full_size_fp64_against_oracle(gpu, oracle):
+    """The clustered workload at the benchmark's size (N = 4,194,304, k = 32,
+    seed 3) with random velocities: one force evaluation of the FP64 form
+    against the oracle's exact evaluation, every array bit for bit."""
+    n = 1 << 22
+    x, y, _, _, u = ics.clustered(n, 3)
+    vx, vy = _moving(n, 3)
+    conf = ics.periodic_config(n, 32, 1e-5, "Exact")
+    o = oracle.OracleSim(oracle_params(oracle, conf, n), x, y, vx, vy, u)
+    g = S.Simulation(conf, x, y, vx, vy, u)
+    g.Autotune()
+    o.forces()
+    g.CalculateForces()
+    os_, gs, gder = o.state(), g.state(), g.derived()
+    oi, od, om = o.neighbours()
+    gi, gd, gm = g.neighbours()
+    assert np.array_equal(gi, oi), np.sum(np.any(gi != oi, axis=1))
+    assert np.array_equal(gm, om) and np.array_equal(gd, od)
+    del oi, od, om, gi, gd, gm
+    for key in STATE:
+        assert np.array_equal(gs[key], os_[key]), key
+    for key in ("rho", "c", "h"):
+        assert np.array_equal(gder[key], os_[key]), key
+    o.close()
+    g.close()
 
 
 def test_clustered_mixed_errors_after_full_run(gpu):
