@@ -425,7 +425,7 @@ int create_impl(const sph_params *params, const int64_t *counts, int32_t nsims, 
     rc |= dalloc(h, &h->d_flags, 1);
     if (rc) return bail(SPH_ERR_NOMEM);
     if (alloc_particles(h, n)) return bail(SPH_ERR_NOMEM);
-    rc |= dalloc(h, &h->D.ndefer, 1);
+    rc |= dalloc(h, &h->D.ndefer, 2);
     h->T.ncells = cells;
     rc |= dalloc(h, &h->T.count, cap);
     rc |= dalloc(h, &h->T.start, cap + 1);

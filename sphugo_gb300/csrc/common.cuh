@@ -88,7 +88,7 @@ struct Derived {
                     // (NNDists, NNDists/h) [bit-exact form] or (NNDists, 1/NNDists) [fast form]
     float *d2f;     // mixed: n*k FP32 squared distances
     int32_t *defer;  // queries the group-tile search leaves to the per-query search (n)
-    int32_t *ndefer; // their count
+    int32_t *ndefer; // their count; ndefer[1]: queries to re-rank, stored from the end of defer
 };
 
 struct Tables {

@@ -1154,6 +1154,42 @@ int knn_tile_occupancy_blocks(int k, int mode) {
     return pick(occ_tile<MODE_MIXED, 1>, occ_tile<MODE_MIXED, 2>, occ_tile<MODE_MIXED, 4>, occ_tile<MODE_MIXED, 8>);
 }
 
+// Queries whose neighbour set the block tiles decided but whose order the
+// FP32 keys could not (two entries within the error bound): their list,
+// written in FP32 order, is sorted by (the reference's FP64 squared distance,
+// particle id, image code), the order the per-query search gives (it sorts
+// the undecided runs by the same key; elsewhere the FP32 order agrees with
+// it). One thread per query; lists of at most kRerankMaxK entries (the block
+// tiles' longest).
+constexpr int kRerankMaxK = 80;
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_rerank(KnnArgs a) {
+    const int k = a.c.k;
+    const int64_t nr = (int64_t)a.D.ndefer[1];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nr; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = a.D.defer[a.c.n - 1 - i];
+        const SimDev &S = a.c.sims[sim_of(a.c, q)];
+        const double2 P = a.B.pos[q];
+        int32_t *out = a.D.nbr + q * k;
+        unsigned long long key[kRerankMaxK];
+        uint32_t code[kRerankMaxK];
+        for (int e = 0; e < k; e++) {  // insertion sort: the list is nearly sorted
+            const uint32_t c = (uint32_t)out[e];
+            const unsigned long long kk = (unsigned long long)__double_as_longlong(nbr_d2(S, a.B, P, c));
+            int f = e - 1;
+            while (f >= 0 && exact_greater(a.B, key[f], code[f], kk, c)) {
+                key[f + 1] = key[f];
+                code[f + 1] = code[f];
+                f--;
+            }
+            key[f + 1] = kk;
+            code[f + 1] = c;
+        }
+        for (int e = 0; e < k; e++) out[e] = (int32_t)code[e];
+    }
+}
+
 bool knn_fuses_density(int k, int mode, const KnnTune &tune) {
     const int nr = list_regs(k);
     return mode == MODE_MIXED && tune.tile && tune.block_warps > 0 && nr <= 4 &&
@@ -1167,8 +1203,12 @@ static void launch_knn_nr(const KnnArgs &args, const Launch &L, const KnnTune &t
     const int resident = L.sms * std::max(tune.blocks_per_sm, 1);
     if (tune.tile && args.D.defer) {
         // group tiles, then the per-query kernel over the deferred queries
-        cudaMemsetAsync(args.D.ndefer, 0, sizeof(int32_t), L.stream);
-        if (!(tune.block_warps > 0 && launch_knn_block(args, L, MODE, NR, tune.block_warps))) {
+        cudaMemsetAsync(args.D.ndefer, 0, 2 * sizeof(int32_t), L.stream);
+        KnnArgs b = args;
+        b.rerank = MODE != MODE_MIXED && args.c.k <= kRerankMaxK ? 1 : 0;
+        if (tune.block_warps > 0 && launch_knn_block(b, L, MODE, NR, tune.block_warps)) {
+            if (b.rerank) k_rerank<MODE><<<L.sms * 4, 128, 0, L.stream>>>(b);
+        } else {
             const int64_t groups = (args.c.n + 31) / 32;
             const int64_t tneed = (groups + kTileWarps - 1) / kTileWarps;
             const int tgrid = (int)std::max<int64_t>(

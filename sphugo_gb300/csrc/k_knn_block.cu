@@ -492,8 +492,16 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
             const float et = kEpsRel * tau + ea;
             ok = ok && tau + 3.f * et <= R2 * (1.f - 4.8e-7f);
             ok = ok && (cnt == k || nxt - tau > 2.f * (kEpsRel * nxt + ea));
-            if (MODE == MODE_MIXED) ok = ok && (k == 1 || tau - prv > 2.f * et);
-            else ok = ok && order_ok;
+            // FP64 forms: a decided set whose order the FP32 keys cannot settle
+            // (two entries within the error bound) is written in FP32 order and
+            // re-sorted by the FP64 keys afterwards (k_rerank), when enabled
+            bool rerank = false;
+            if (MODE == MODE_MIXED) {
+                ok = ok && (k == 1 || tau - prv > 2.f * et);
+            } else {
+                rerank = a.rerank && ok && !order_ok;
+                ok = ok && (order_ok || rerank);
+            }
             // Outputs go out four entries per store (each list row is 16-byte
             // aligned: q k 4 bytes with k a multiple of four).
             bool stored = false;
@@ -599,6 +607,7 @@ __global__ void __launch_bounds__(WARPS * 32, WARPS == 8 ? (NR <= 2 ? 3 : 1) : (
                 }
             }
             defer_lanes(a, valid && !ok, q, lane);
+            if (MODE != MODE_MIXED) rerank_lanes(a, valid && rerank, q, lane);
             __syncthreads();  // every thread is done with the rows and the tile
             for (int r = tid; r < kRowCap; r += NT) {  // rows reset for the next pass
                 sm.rx0[r] = INT_MAX;

@@ -15,6 +15,7 @@ struct KnnArgs {
     float theta, hgrow;
     int use_defer;  // per-query kernel / density: walk the deferred list instead of every particle
     int fuse_density;  // mixed block tiles: each settled query's density computed with its list
+    int rerank;  // FP64 forms, block tiles: a decided set whose order needs FP64 goes to the re-rank list
 };
 
 // |d2_f32 - d2_ref| <= kEpsRel * d2 + eps_abs(R): the float-pair difference
@@ -85,6 +86,18 @@ __device__ __forceinline__ void defer_lanes(const KnnArgs &a, bool mine, int64_t
     if (lane == 0) base = atomicAdd(a.D.ndefer, __popc(bal));
     base = __shfl_sync(0xffffffffu, base, 0);
     if (mine) a.D.defer[base + __popc(bal & lanemask_lt())] = (int32_t)q;
+}
+
+// appends the lanes' queries to the re-rank list, stored from the end of the
+// deferred-query array (a query is in at most one of the two lists), counted
+// in ndefer[1]
+__device__ __forceinline__ void rerank_lanes(const KnnArgs &a, bool mine, int64_t q, int lane) {
+    const uint32_t bal = __ballot_sync(0xffffffffu, mine);
+    if (!bal) return;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(a.D.ndefer + 1, __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (mine) a.D.defer[a.c.n - 1 - (base + __popc(bal & lanemask_lt()))] = (int32_t)q;
 }
 
 // the reference's squared distance to the neighbour image a list code names
