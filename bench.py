@@ -98,7 +98,7 @@ FP64_NOTE = ("the density computes its multiplications, square roots and divisio
              "multiplications and divisions, with integer instructions beside the FP64 unit (bit-identical "
              "to the hardware instructions; sph_selftest_fp64emu), so frac can exceed 1 against the FP64 "
              "unit's issue ceiling; ncu on the clustered workload at N = 1,048,576: force FP64 pipe 67 %, "
-             "ALU pipe 52 %, issue slots 56 % busy; density 76 %, 57 %, 58 %")
+             "ALU pipe 52 %, issue slots 56 % busy; density 72 %, 62 %, 63 %")
 
 
 def algorithmic(k, div, sqrt, lo_frac, visc_frac):
