@@ -121,6 +121,9 @@ int main(int argc, char **argv) {
         if (cls == 1 && ((r3 >> 24) & 1u)) {
             const double q = emu_double((1023ull << 52) | (r1 & kEmuFrac));
             num = emu_double(emu_bits(y * q) + (uint64_t)((int64_t)((r2 >> 5) % 5u) - 2));
+        } else if (cls == 2) {  // exact quotients: short significands multiplied back
+            const double q = emu_double((1023ull << 52) | (r1 & 0x000FFFFFFC000000ull));
+            num = y * q;
         }
         if (!same(emu_div(num, emu_divisor(den), den), num / den)) bad[3]++;
         // square roots: the operand, and squares moved by -2 .. +2 ulp
@@ -128,6 +131,9 @@ int main(int argc, char **argv) {
         if (cls == 1 || cls == 4) {
             const double sq = emu_double(((uint64_t)(512u + (uint32_t)(r3 % 1024u)) << 52) | (r1 & kEmuFrac));
             z = emu_double(emu_bits(sq * sq) + (uint64_t)((int64_t)((r2 >> 3) % 5u) - 2));
+        } else if (cls == 2) {  // perfect squares
+            const double sq = emu_double(((uint64_t)(512u + (uint32_t)(r3 % 1024u)) << 52) | (r1 & 0x000FFFFFFC000000ull));
+            z = sq * sq;
         }
         if (!same(emu_sqrt(z), std::sqrt(z))) bad[4]++;
         const double xh = emu_double((1022ull << 52) | (r1 & kEmuFrac));
